@@ -1,0 +1,108 @@
+"""ctypes binding of ``libcyclix_gpu.so`` (declarations in ``include/cyclix_gpu.h``).
+
+Loading fails loudly: there is no CPU implementation behind these names.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "libcyclix_gpu.so"
+
+CX_OK, CX_ERR_ARG, CX_ERR_CUDA, CX_ERR_NOMEM, CX_ERR_LIB, CX_ERR_NOTPD, CX_ERR_STATE, CX_ERR_NOCONV = range(8)
+CX_PREC_FP64, CX_PREC_MIXED = 0, 1
+PREC = {"fp64": CX_PREC_FP64, "mixed": CX_PREC_MIXED}
+
+EXPORTS = ["cx_create", "cx_destroy", "cx_last_error", "cx_version", "cx_set_blocks", "cx_set_veff", "cx_set_psi",
+           "cx_get_psi", "cx_hpsi", "cx_chebyshev_filter", "cx_eigsolver", "cx_eigsolver_host", "cx_poisson", "cx_sync",
+           "cx_timer_start", "cx_timer_stop", "cx_profile_stencil", "cx_profile_read", "cx_launch_count"]
+
+
+class cx_grid(C.Structure):
+    _fields_ = [("Nx", C.c_int32), ("Ny", C.c_int32), ("Nz", C.c_int32), ("FDn", C.c_int32), ("cell_typ", C.c_int32),
+                ("BCx", C.c_int32), ("BCy", C.c_int32), ("BCz", C.c_int32),
+                ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double), ("xin", C.c_double), ("twist", C.c_double),
+                ("L1", C.c_double), ("L2", C.c_double), ("L3", C.c_double),
+                ("w1", C.POINTER(C.c_double)), ("w2", C.POINTER(C.c_double)), ("W", C.POINTER(C.c_double))]
+
+
+class cx_rc_image(C.Structure):
+    _fields_ = [("rc_n_nodes", C.c_int32), ("rc_pos", C.POINTER(C.c_int64)), ("Chi_mat", C.POINTER(C.c_double)),
+                ("coordinates", C.c_double * 3)]
+
+
+class cx_atom(C.Structure):
+    _fields_ = [("angnum", C.c_int32), ("n_image_rc", C.c_int32), ("gamma_Jl", C.POINTER(C.c_double)),
+                ("position", C.c_double * 3), ("rcImage", C.POINTER(cx_rc_image))]
+
+
+class cx_block(C.Structure):
+    _fields_ = [("kpt_vec", C.c_double * 3), ("spin", C.c_int32), ("Ns", C.c_int32)]
+
+
+_lib = None
+
+
+def load(build_if_missing: bool = True):
+    """Load the library (building it in-tree first when it is missing or stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing:
+        from .build import build
+        build()
+    if not LIB_PATH.exists():
+        raise ImportError(f"libcyclix_gpu.so not found at {LIB_PATH}; run cyclix_msparc_gb300.build")
+    lib = C.CDLL(str(LIB_PATH))
+    P = C.POINTER
+    dp = P(C.c_double)
+    h = C.c_void_p
+    sig = {
+        "cx_create": ([P(cx_grid), C.c_int32, P(cx_atom), C.c_int32, P(C.c_void_p)], C.c_int32),
+        "cx_destroy": ([h], C.c_int32),
+        "cx_last_error": ([h], C.c_char_p),
+        "cx_version": ([], C.c_char_p),
+        "cx_set_blocks": ([h, C.c_int32, P(cx_block), C.c_int32], C.c_int32),
+        "cx_set_veff": ([h, dp], C.c_int32),
+        "cx_set_psi": ([h, C.c_int32, dp], C.c_int32),
+        "cx_get_psi": ([h, C.c_int32, dp], C.c_int32),
+        "cx_hpsi": ([h, C.c_int32, C.c_int32, dp, dp, C.c_int32], C.c_int32),
+        "cx_chebyshev_filter": ([h, C.c_int32, C.c_int32, dp, dp, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_int32],
+                                C.c_int32),
+        "cx_eigsolver": ([h, C.c_int32, C.c_int32, C.c_int32, dp, dp, dp, dp], C.c_int32),
+        "cx_eigsolver_host": ([h, C.c_int32, C.c_int32, C.c_int32, dp, dp, dp, dp, dp], C.c_int32),
+        "cx_poisson": ([h, dp, dp, C.c_double, C.c_int32, C.c_int32, P(C.c_int32), dp], C.c_int32),
+        "cx_sync": ([h], C.c_int32),
+        "cx_timer_start": ([h], C.c_int32),
+        "cx_timer_stop": ([h, dp], C.c_int32),
+        "cx_profile_stencil": ([h, C.c_int32], C.c_int32),
+        "cx_profile_read": ([h, P(C.c_int64), dp, dp], C.c_int32),
+        "cx_launch_count": ([h, P(C.c_int64), C.c_int32], C.c_int32),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = lib
+    return lib
+
+
+class CxError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"cyclix_gpu status {status}: {msg}")
+        self.status = status
+
+
+def dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def check(lib, h, status):
+    if status != CX_OK:
+        msg = lib.cx_last_error(h)
+        raise CxError(status, msg.decode() if msg else "")
+    return status

@@ -1,0 +1,610 @@
+// C-ABI entry points of libcyclix_gpu.so: handle lifecycle, operator tables, block
+// buffers, host <-> device transfers, H*psi and the Chebyshev filter.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <algorithm>
+#include <complex>
+
+#include "cx_internal.h"
+#include "cx_common.h"
+
+namespace {
+thread_local std::string g_create_err;
+
+template <typename T>
+cx_status dalloc(cx_handle h, T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    h->err = std::string("cudaMalloc(") + std::to_string(count * sizeof(T)) + " B): " + cudaGetErrorString(e);
+    *p = nullptr;
+    return CX_ERR_NOMEM;
+  }
+  return CX_OK;
+}
+
+template <typename T>
+cx_status upload(cx_handle h, T** p, const std::vector<T>& v) {
+  cx_status s = dalloc(h, p, v.size());
+  if (s != CX_OK) return s;
+  if (!v.empty()) CX_TRY_CUDA(h, cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  h->nl_allocs.push_back((void*)*p);
+  return CX_OK;
+}
+
+double2 cexp_i(double ang) { return make_double2(std::cos(ang), std::sin(ang)); }
+
+void free_blocks(cx_handle h) {
+  for (void* p : h->bufs) cudaFree(p);
+  h->bufs.clear();
+  for (void* p : h->ubgv) cudaFree(p);
+  h->ubgv.clear();
+  cudaFree(h->d_blocks); h->d_blocks = nullptr;
+  cudaFree(h->d_state_tab); h->d_state_tab = nullptr;
+  cudaFree(h->d_cprime); h->d_cprime = nullptr;
+  cudaFree(h->d_seg_phase); h->d_seg_phase = nullptr;
+  h->nl.seg_phase = nullptr;
+  h->nblk = 0;
+  h->nstates = 0;
+  h->blocks.clear();
+  h->state0.clear();
+}
+}  // namespace
+
+namespace cx {
+
+// Device array of BlockDev<R> for the handle's blocks with the given buffer pointers.
+template <typename R>
+cx_status make_block_devs(cx_handle h, const std::vector<cplx<R>*>& b0, const std::vector<cplx<R>*>& b1,
+                          const std::vector<int>& blk_ids, std::vector<BlockDev<R>>& out) {
+  out.clear();
+  int st = 0;
+  for (size_t i = 0; i < blk_ids.size(); ++i) {
+    const cx_block& B = h->blocks[blk_ids[i]];
+    BlockDev<R> d{};
+    d.buf[0] = b0[i];
+    d.buf[1] = b1[i];
+    d.veff = h->d_veff + (size_t)B.spin * h->g.N;
+    const double k2 = B.kpt_vec[1], k3 = B.kpt_vec[2];
+    d.ph_tl = k2 == 0 ? make_double2(1, 0) : cexp_i(-k2 * h->grid.L2);
+    d.ph_tr = k2 == 0 ? make_double2(1, 0) : cexp_i(k2 * h->grid.L2);
+    d.ph_zl = k3 == 0 ? make_double2(1, 0) : cexp_i(-k3 * h->grid.L3);
+    d.ph_zr = k3 == 0 ? make_double2(1, 0) : cexp_i(k3 * h->grid.L3);
+    d.Ns = B.Ns;
+    d.state0 = st;
+    st += B.Ns;
+    out.push_back(d);
+  }
+  return CX_OK;
+}
+
+// Per-block phases exp(i k.(R_J - R_img)) of every (atom, image) segment (src/h_nonlocal_vector_mult.m:24-28,33).
+std::vector<double2> segment_phases(cx_handle h, const cx_block& B) {
+  const int nseg = (int)h->seg_atom.size();
+  std::vector<double2> ph(nseg);
+  const bool gamma = B.kpt_vec[0] == 0 && B.kpt_vec[1] == 0 && B.kpt_vec[2] == 0;
+  for (int s = 0; s < nseg; ++s) {
+    if (gamma) { ph[s] = make_double2(1, 0); continue; }
+    const int J = h->seg_atom[s];
+    double dot = 0;
+    for (int d = 0; d < 3; ++d) dot += B.kpt_vec[d] * (h->atom_pos[3 * J + d] - h->seg_coord[3 * s + d]);
+    ph[s] = cexp_i(dot);
+  }
+  return ph;
+}
+
+// Chebyshev scalars of src/chebyshev_filter.m:19-42 for degrees 1..m.
+void cheb_scalars(int m, double a, double b, double a0, std::vector<StepScalars>& out, int stride, int col) {
+  const double e = (b - a) / 2, c = (b + a) / 2;
+  double sigma = e / (a0 - c);
+  const double sigma1 = sigma, gamma = 2 / sigma1;
+  out[(size_t)0 * stride + col] = StepScalars{sigma1 / e, c, 0.0, 0.0};
+  for (int d = 2; d <= m; ++d) {
+    const double sigma2 = 1 / (gamma - sigma);
+    out[(size_t)(d - 1) * stride + col] = StepScalars{2 * sigma2 / e, c, -(sigma * sigma2), 0.0};
+    sigma = sigma2;
+  }
+}
+
+// Launch one fused step over the given block set and account profiling.
+template <typename R>
+cx_status fused_step(cx_handle h, const BlockDev<R>* d_blocks, const StepScalars* d_scal, int nblk, const int2* d_state_tab,
+                     int nstates, int in_sel, bool use_xprev, cplx<R>* cprime, bool nonlocal, double bytes) {
+  const NonlocalDev* nlp = nullptr;
+  NonlocalDev nl = h->nl;
+  if (nonlocal && nl.nseg > 0) {
+    nl.node_wchi = sizeof(R) == 4 ? h->d_node_wchi32 : h->d_node_wchi64;
+    nl.ent_chi = sizeof(R) == 4 ? h->d_ent_chi32 : h->d_ent_chi64;
+    CX_TRY_CUDA(h, launch_nl_contract<R>(h->g, d_blocks, d_state_tab, nstates, in_sel, nl, cprime, h->stream));
+    h->launches++;
+    nlp = &nl;
+  }
+  if (h->prof) CX_TRY_CUDA(h, cudaEventRecord(h->ev0, h->stream));
+  CX_TRY_CUDA(h, launch_cheb_step<R>(h->g, h->coef, d_blocks, d_scal, nblk, d_state_tab, nstates, in_sel, use_xprev, nlp,
+                                     cprime, h->stream));
+  h->launches++;
+  if (h->prof) {
+    CX_TRY_CUDA(h, cudaEventRecord(h->ev1, h->stream));
+    CX_TRY_CUDA(h, cudaEventSynchronize(h->ev1));
+    float ms = 0;
+    CX_TRY_CUDA(h, cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+    h->prof_ms += ms;
+    h->prof_launches++;
+    h->prof_bytes += bytes;
+  }
+  return CX_OK;
+}
+
+// Filter degree m on all blocks of the set; psi in buffer sel0, result buffer returned in *sel_out.
+template <typename R>
+cx_status filter_blocks(cx_handle h, const BlockDev<R>* d_blocks, int nblk, const int2* d_state_tab, int nstates,
+                        size_t total_elems, int sel0, int m, const std::vector<double>& a, const std::vector<double>& b,
+                        const std::vector<double>& a0, cplx<R>* cprime, int* sel_out) {
+  if (m < 1) { h->err = "filter degree must be >= 1"; return CX_ERR_ARG; }
+  std::vector<StepScalars> sc((size_t)m * nblk);
+  for (int i = 0; i < nblk; ++i) cheb_scalars(m, a[i], b[i], a0[i], sc, nblk, i);
+  if (h->scal_cap < m * nblk) {
+    cudaFree(h->d_scal);
+    h->d_scal = nullptr;
+    h->scal_cap = 0;
+    cx_status s = dalloc(h, &h->d_scal, (size_t)m * nblk);
+    if (s != CX_OK) return s;
+    h->scal_cap = m * nblk;
+  }
+  CX_TRY_CUDA(h, cudaMemcpyAsync(h->d_scal, sc.data(), sc.size() * sizeof(StepScalars), cudaMemcpyHostToDevice, h->stream));
+  const double sz = (double)total_elems * sizeof(cplx<R>);
+  for (int d = 1; d <= m; ++d) {
+    const int in_sel = sel0 ^ ((d - 1) & 1);
+    cx_status s = fused_step<R>(h, d_blocks, h->d_scal + (size_t)(d - 1) * nblk, nblk, d_state_tab, nstates, in_sel, d >= 2,
+                                cprime, true, (d >= 2 ? 3.0 : 2.0) * sz);
+    if (s != CX_OK) return s;
+  }
+  *sel_out = sel0 ^ (m & 1);
+  return CX_OK;
+}
+
+template cx_status filter_blocks<float>(cx_handle, const BlockDev<float>*, int, const int2*, int, size_t, int, int,
+                                        const std::vector<double>&, const std::vector<double>&, const std::vector<double>&,
+                                        cplx<float>*, int*);
+template cx_status filter_blocks<double>(cx_handle, const BlockDev<double>*, int, const int2*, int, size_t, int, int,
+                                         const std::vector<double>&, const std::vector<double>&, const std::vector<double>&,
+                                         cplx<double>*, int*);
+template cx_status make_block_devs<float>(cx_handle, const std::vector<cplx<float>*>&, const std::vector<cplx<float>*>&,
+                                          const std::vector<int>&, std::vector<BlockDev<float>>&);
+template cx_status make_block_devs<double>(cx_handle, const std::vector<cplx<double>*>&, const std::vector<cplx<double>*>&,
+                                           const std::vector<int>&, std::vector<BlockDev<double>>&);
+template cx_status fused_step<float>(cx_handle, const BlockDev<float>*, const StepScalars*, int, const int2*, int, int, bool,
+                                     cplx<float>*, bool, double);
+template cx_status fused_step<double>(cx_handle, const BlockDev<double>*, const StepScalars*, int, const int2*, int, int, bool,
+                                      cplx<double>*, bool, double);
+
+// A one-block scratch view (used by the host-buffer entry points): temporary buffers of ncol columns.
+template <typename R>
+struct ScratchView {
+  cplx<R>* b0 = nullptr;
+  cplx<R>* b1 = nullptr;
+  cplx<R>* cprime = nullptr;
+  BlockDev<R>* d_blk = nullptr;
+  int2* d_tab = nullptr;
+  StepScalars* d_scal = nullptr;
+  double2* d_ph = nullptr;
+  double2* saved_ph = nullptr;
+  ~ScratchView() {
+    cudaFree(b0); cudaFree(b1); cudaFree(cprime); cudaFree(d_blk); cudaFree(d_tab); cudaFree(d_scal); cudaFree(d_ph);
+  }
+};
+
+template <typename R>
+cx_status make_scratch(cx_handle h, int blk, int ncol, ScratchView<R>& v) {
+  const size_t N = h->g.N;
+  cx_status s;
+  if ((s = dalloc(h, &v.b0, N * ncol)) != CX_OK) return s;
+  if ((s = dalloc(h, &v.b1, N * ncol)) != CX_OK) return s;
+  const int nseg = std::max(1, h->nl.nseg);
+  if ((s = dalloc(h, &v.cprime, (size_t)ncol * nseg * kAngMax)) != CX_OK) return s;
+  if ((s = dalloc(h, &v.d_blk, 1)) != CX_OK) return s;
+  if ((s = dalloc(h, &v.d_tab, ncol)) != CX_OK) return s;
+  if ((s = dalloc(h, &v.d_ph, nseg)) != CX_OK) return s;
+  std::vector<BlockDev<R>> bd;
+  std::vector<cplx<R>*> p0{v.b0}, p1{v.b1};
+  make_block_devs<R>(h, p0, p1, std::vector<int>{blk}, bd);
+  bd[0].Ns = ncol;
+  CX_TRY_CUDA(h, cudaMemcpy(v.d_blk, bd.data(), sizeof(BlockDev<R>), cudaMemcpyHostToDevice));
+  std::vector<int2> tab(ncol);
+  for (int i = 0; i < ncol; ++i) tab[i] = make_int2(0, i);
+  CX_TRY_CUDA(h, cudaMemcpy(v.d_tab, tab.data(), sizeof(int2) * ncol, cudaMemcpyHostToDevice));
+  std::vector<double2> ph = segment_phases(h, h->blocks[blk]);
+  if (!ph.empty()) CX_TRY_CUDA(h, cudaMemcpy(v.d_ph, ph.data(), sizeof(double2) * ph.size(), cudaMemcpyHostToDevice));
+  return CX_OK;
+}
+
+template <typename R>
+static cx_status hpsi_T(cx_handle h, int blk, int ncol, const double* X, double* Y) {
+  ScratchView<R> v;
+  cx_status s = make_scratch<R>(h, blk, ncol, v);
+  if (s != CX_OK) return s;
+  const size_t n = (size_t)h->g.N * ncol;
+  if ((s = cx_host_to_dev(h, X, v.b0, n, sizeof(R) == 8 ? CX_PREC_FP64 : CX_PREC_MIXED)) != CX_OK) return s;
+  StepScalars one{1.0, 0.0, 0.0, 0.0};
+  if ((s = dalloc(h, &v.d_scal, 1)) != CX_OK) return s;
+  CX_TRY_CUDA(h, cudaMemcpy(v.d_scal, &one, sizeof(one), cudaMemcpyHostToDevice));
+  const double2* saved = h->nl.seg_phase;
+  h->nl.seg_phase = v.d_ph;
+  s = fused_step<R>(h, v.d_blk, v.d_scal, 1, v.d_tab, ncol, 0, false, v.cprime, true, 2.0 * n * sizeof(cplx<R>));
+  h->nl.seg_phase = saved;
+  if (s != CX_OK) return s;
+  return cx_dev_to_host(h, v.b1, Y, n, sizeof(R) == 8 ? CX_PREC_FP64 : CX_PREC_MIXED);
+}
+
+template <typename R>
+static cx_status filter_T(cx_handle h, int blk, int ncol, const double* X, double* Y, int m, double a, double b, double a0) {
+  ScratchView<R> v;
+  cx_status s = make_scratch<R>(h, blk, ncol, v);
+  if (s != CX_OK) return s;
+  const size_t n = (size_t)h->g.N * ncol;
+  const int pr = sizeof(R) == 8 ? CX_PREC_FP64 : CX_PREC_MIXED;
+  if ((s = cx_host_to_dev(h, X, v.b0, n, pr)) != CX_OK) return s;
+  const double2* saved = h->nl.seg_phase;
+  h->nl.seg_phase = v.d_ph;
+  StepScalars* saved_scal = h->d_scal;
+  int saved_cap = h->scal_cap;
+  h->d_scal = nullptr;
+  h->scal_cap = 0;
+  int sel = 0;
+  s = filter_blocks<R>(h, v.d_blk, 1, v.d_tab, ncol, n, 0, m, std::vector<double>{a}, std::vector<double>{b},
+                       std::vector<double>{a0}, v.cprime, &sel);
+  v.d_scal = h->d_scal;            // freed with the view
+  h->d_scal = saved_scal;
+  h->scal_cap = saved_cap;
+  h->nl.seg_phase = saved;
+  if (s != CX_OK) return s;
+  return cx_dev_to_host(h, sel ? v.b1 : v.b0, Y, n, pr);
+}
+
+}  // namespace cx
+
+using namespace cx;
+
+extern "C" {
+
+const char* cx_version(void) { return "cyclix_gpu 0.1 (sm_103a)"; }
+
+const char* cx_last_error(cx_handle h) { return h ? h->err.c_str() : g_create_err.c_str(); }
+
+cx_status cx_create(const cx_grid* grid, int32_t n_atm, const cx_atom* atoms, int32_t nspin, cx_handle* out) {
+  if (!out) { g_create_err = "cx_create: out is NULL"; return CX_ERR_ARG; }
+  *out = nullptr;
+  if (!grid || !grid->w1 || !grid->w2 || !grid->W) { g_create_err = "cx_create: grid, w1, w2, W required"; return CX_ERR_ARG; }
+  const cx_grid& G = *grid;
+  if (G.FDn < 1 || G.FDn > kMaxFDn) { g_create_err = "cx_create: FDn must be in 1..8"; return CX_ERR_ARG; }
+  if (G.cell_typ < 3 || G.cell_typ > 5) { g_create_err = "cx_create: cell_typ must be 3 (cyclic) or 4/5 (helical)"; return CX_ERR_ARG; }
+  if (G.BCx != 1) { g_create_err = "cx_create: the radial direction must be Dirichlet (BCx = 1)"; return CX_ERR_ARG; }
+  if (G.Nx < 1 || G.Ny <= G.FDn || G.Nz <= G.FDn) {
+    g_create_err = "cx_create: need Nx >= 1 and Ny, Nz > FDn (one Bloch wrap per stencil)";
+    return CX_ERR_ARG;
+  }
+  if ((G.cell_typ == 4 || G.cell_typ == 5) && G.twist == 0) { g_create_err = "cx_create: helical cell needs twist != 0"; return CX_ERR_ARG; }
+  if (nspin < 1 || nspin > 2) { g_create_err = "cx_create: nspin must be 1 or 2"; return CX_ERR_ARG; }
+  if (n_atm < 0 || (n_atm > 0 && !atoms)) { g_create_err = "cx_create: atoms required"; return CX_ERR_ARG; }
+  const long long Nll = (long long)G.Nx * G.Ny * G.Nz;
+  if (Nll >= (1LL << 31)) { g_create_err = "cx_create: grid too large (N must fit int32)"; return CX_ERR_ARG; }
+
+  cx_handle h = new cx_handle_s();
+  h->grid = G;
+  h->nspin = nspin;
+  const int N = (int)Nll;
+  h->g.Nx = G.Nx; h->g.Ny = G.Ny; h->g.Nz = G.Nz; h->g.N = N;
+  h->g.FDn = G.FDn; h->g.helical = (G.cell_typ != 3); h->g.BCy = G.BCy; h->g.BCz = G.BCz;
+  h->g.xin = G.xin; h->g.dx = G.dx; h->g.twist = G.twist;
+  // 1-D stencil coefficients (Cychel/lapIndicesValues_1d_cychel.m:30-46,165-173,191-201,229-239)
+  for (int q = 0; q <= G.FDn; ++q) {
+    h->coef.cr2[q] = G.w2[q] / (G.dx * G.dx);
+    h->coef.cr1[q] = q == 0 ? 0.0 : G.w1[q] / G.dx;
+    h->coef.ct2[q] = G.w2[q] / (G.dy * G.dy);
+    h->coef.ct1[q] = q == 0 ? 0.0 : -2.0 * G.twist * G.w1[q] / G.dy;
+    h->coef.cz2[q] = G.w2[q] / (G.dz * G.dz);
+    h->coef.cz1[q] = q == 0 ? 0.0 : G.w1[q] / G.dz;
+  }
+  h->W.assign(G.W, G.W + N);
+  cudaError_t e;
+  if ((e = cudaGetDevice(&h->dev)) != cudaSuccess || (e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+    g_create_err = std::string("cx_create: CUDA unavailable: ") + cudaGetErrorString(e);
+    delete h;
+    return CX_ERR_CUDA;
+  }
+  cudaEventCreate(&h->ev0); cudaEventCreate(&h->ev1); cudaEventCreate(&h->tev0); cudaEventCreate(&h->tev1);
+  if (cublasCreate(&h->cublas) != CUBLAS_STATUS_SUCCESS || cublasSetStream(h->cublas, h->stream) != CUBLAS_STATUS_SUCCESS) {
+    g_create_err = "cx_create: cublasCreate failed";
+    cx_destroy(h);
+    return CX_ERR_LIB;
+  }
+  if (cusolverDnCreate(&h->cusolver) != CUSOLVER_STATUS_SUCCESS || cusolverDnSetStream(h->cusolver, h->stream) != CUSOLVER_STATUS_SUCCESS ||
+      cusolverDnCreateParams(&h->cusolver_params) != CUSOLVER_STATUS_SUCCESS) {
+    g_create_err = "cx_create: cusolverDnCreate failed";
+    cx_destroy(h);
+    return CX_ERR_LIB;
+  }
+  cx_status s;
+  if ((s = upload(h, &h->d_W, h->W)) != CX_OK) { g_create_err = h->err; cx_destroy(h); return s; }
+  if ((s = dalloc(h, &h->d_veff, (size_t)N * nspin)) != CX_OK) { g_create_err = h->err; cx_destroy(h); return s; }
+  CX_TRY_CUDA(h, cudaMemset(h->d_veff, 0, sizeof(double) * (size_t)N * nspin));
+
+  // ---- nonlocal tables
+  std::vector<int32_t> atom_node_ptr(1, 0), node_pos, node_seg, atom_seg_ptr(1, 0), angn;
+  std::vector<double> node_wchi, gam;
+  std::vector<int32_t> ent_count(N, 0);
+  for (int J = 0; J < n_atm; ++J) {
+    const cx_atom& A = atoms[J];
+    if (A.angnum < 0 || A.angnum > kAngMax || A.n_image_rc < 0 || (A.n_image_rc > 0 && !A.rcImage) || (A.angnum > 0 && !A.gamma_Jl)) {
+      g_create_err = "cx_create: atom " + std::to_string(J) + ": angnum must be 0..4 and rcImage/gamma_Jl given";
+      cx_destroy(h);
+      return CX_ERR_ARG;
+    }
+    for (int d = 0; d < 3; ++d) h->atom_pos.push_back(A.position[d]);
+    for (int q = 0; q < kAngMax; ++q) gam.push_back(q < A.angnum ? A.gamma_Jl[q] : 0.0);
+    angn.push_back(A.angnum);
+    for (int im = 0; im < A.n_image_rc; ++im) {
+      const cx_rc_image& I = A.rcImage[im];
+      const int seg = (int)h->seg_atom.size();
+      h->seg_atom.push_back(J);
+      for (int d = 0; d < 3; ++d) h->seg_coord.push_back(I.coordinates[d]);
+      if (I.rc_n_nodes < 0 || (I.rc_n_nodes > 0 && (!I.rc_pos || !I.Chi_mat))) {
+        g_create_err = "cx_create: image without rc_pos / Chi_mat";
+        cx_destroy(h);
+        return CX_ERR_ARG;
+      }
+      for (int n = 0; n < I.rc_n_nodes; ++n) {
+        const int64_t pos = I.rc_pos[n] - 1;
+        if (pos < 0 || pos >= N) {
+          g_create_err = "cx_create: rc_pos out of range (atom " + std::to_string(J) + ")";
+          cx_destroy(h);
+          return CX_ERR_ARG;
+        }
+        node_pos.push_back((int32_t)pos);
+        node_seg.push_back(seg);
+        for (int q = 0; q < kAngMax; ++q)
+          node_wchi.push_back(q < A.angnum ? h->W[pos] * I.Chi_mat[(size_t)q * I.rc_n_nodes + n] : 0.0);
+        ent_count[pos]++;
+      }
+    }
+    atom_node_ptr.push_back((int32_t)node_pos.size());
+    atom_seg_ptr.push_back((int32_t)h->seg_atom.size());
+  }
+  // per-point CSR of (segment, Chi) entries for the fused apply
+  std::vector<int32_t> row_ptr(N + 1, 0);
+  for (int p = 0; p < N; ++p) row_ptr[p + 1] = row_ptr[p] + ent_count[p];
+  const size_t nent = row_ptr[N];
+  std::vector<int32_t> ent_seg(nent), fill(row_ptr.begin(), row_ptr.end() - 1);
+  std::vector<double> ent_chi(nent * kAngMax, 0.0);
+  {
+    size_t n = 0;
+    for (int J = 0; J < n_atm; ++J) {
+      const cx_atom& A = atoms[J];
+      for (int im = 0; im < A.n_image_rc; ++im) {
+        const cx_rc_image& I = A.rcImage[im];
+        for (int k = 0; k < I.rc_n_nodes; ++k, ++n) {
+          const int p = node_pos[n];
+          const int slot = fill[p]++;
+          ent_seg[slot] = node_seg[n];
+          for (int q = 0; q < A.angnum; ++q) ent_chi[(size_t)slot * kAngMax + q] = I.Chi_mat[(size_t)q * I.rc_n_nodes + k];
+        }
+      }
+    }
+  }
+  h->nl.n_atm = n_atm;
+  h->nl.nseg = (int)h->seg_atom.size();
+  h->nl.nnode = (int)node_pos.size();
+  std::vector<float> node_wchi32(node_wchi.begin(), node_wchi.end()), ent_chi32(ent_chi.begin(), ent_chi.end());
+  int32_t *d_anp, *d_np, *d_ns, *d_asp, *d_an, *d_rp, *d_es;
+  double *d_g, *d_w64, *d_c64;
+  float *d_w32, *d_c32;
+  if ((s = upload(h, &d_anp, atom_node_ptr)) || (s = upload(h, &d_np, node_pos)) || (s = upload(h, &d_ns, node_seg)) ||
+      (s = upload(h, &d_asp, atom_seg_ptr)) || (s = upload(h, &d_an, angn)) || (s = upload(h, &d_rp, row_ptr)) ||
+      (s = upload(h, &d_es, ent_seg)) || (s = upload(h, &d_g, gam)) || (s = upload(h, &d_w64, node_wchi)) ||
+      (s = upload(h, &d_c64, ent_chi)) || (s = upload(h, &d_w32, node_wchi32)) || (s = upload(h, &d_c32, ent_chi32))) {
+    g_create_err = h->err;
+    cx_destroy(h);
+    return s;
+  }
+  h->nl.atom_node_ptr = d_anp; h->nl.node_pos = d_np; h->nl.node_seg = d_ns; h->nl.atom_seg_ptr = d_asp;
+  h->nl.angnum = d_an; h->nl.row_ptr = d_rp; h->nl.ent_seg = d_es; h->nl.gamma = d_g;
+  h->d_node_wchi64 = d_w64; h->d_ent_chi64 = d_c64; h->d_node_wchi32 = d_w32; h->d_ent_chi32 = d_c32;
+  *out = h;
+  return CX_OK;
+}
+
+cx_status cx_destroy(cx_handle h) {
+  if (!h) return CX_OK;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  free_blocks(h);
+  for (void* p : h->nl_allocs) cudaFree(p);
+  cudaFree(h->d_veff);
+  cudaFree(h->d_scal);
+  cudaFree(h->d_ws);
+  cudaFreeHost(h->h_ws);
+  cx_free_extra(h);
+  if (h->cusolver_params) cusolverDnDestroyParams(h->cusolver_params);
+  if (h->cusolver) cusolverDnDestroy(h->cusolver);
+  if (h->cublas) cublasDestroy(h->cublas);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->tev0) cudaEventDestroy(h->tev0);
+  if (h->tev1) cudaEventDestroy(h->tev1);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return CX_OK;
+}
+
+cx_status cx_set_veff(cx_handle h, const double* Veff) {
+  if (!h || !Veff) return CX_ERR_ARG;
+  CX_TRY_CUDA(h, cudaMemcpyAsync(h->d_veff, Veff, sizeof(double) * (size_t)h->g.N * h->nspin, cudaMemcpyHostToDevice, h->stream));
+  CX_TRY_CUDA(h, cudaStreamSynchronize(h->stream));
+  return CX_OK;
+}
+
+cx_status cx_set_blocks(cx_handle h, int32_t nblk, const cx_block* blocks, int32_t prec) {
+  if (!h) return CX_ERR_ARG;
+  if (nblk < 1 || !blocks) { h->err = "cx_set_blocks: need nblk >= 1 blocks"; return CX_ERR_ARG; }
+  if (prec != CX_PREC_FP64 && prec != CX_PREC_MIXED) { h->err = "cx_set_blocks: prec must be CX_PREC_FP64 or CX_PREC_MIXED"; return CX_ERR_ARG; }
+  int total = 0;
+  for (int b = 0; b < nblk; ++b) {
+    if (blocks[b].Ns < 1 || blocks[b].spin < 0 || blocks[b].spin >= h->nspin) {
+      h->err = "cx_set_blocks: block " + std::to_string(b) + " needs Ns >= 1 and 0 <= spin < nspin";
+      return CX_ERR_ARG;
+    }
+    total += blocks[b].Ns;
+  }
+  if (total > 65535) { h->err = "cx_set_blocks: at most 65535 states in total"; return CX_ERR_ARG; }
+  CX_TRY_CUDA(h, cudaStreamSynchronize(h->stream));
+  free_blocks(h);
+  h->prec = prec;
+  h->nblk = nblk;
+  h->blocks.assign(blocks, blocks + nblk);
+  const size_t N = h->g.N;
+  const size_t cs = prec == CX_PREC_FP64 ? sizeof(double2) : sizeof(float2);
+  std::vector<int2> tab;
+  for (int b = 0; b < nblk; ++b) {
+    h->state0.push_back(h->nstates);
+    for (int i = 0; i < blocks[b].Ns; ++i) tab.push_back(make_int2(b, i));
+    h->nstates += blocks[b].Ns;
+    for (int k = 0; k < 2; ++k) {
+      void* p = nullptr;
+      cudaError_t e = cudaMalloc(&p, N * blocks[b].Ns * cs);
+      if (e != cudaSuccess) { h->err = std::string("cx_set_blocks: psi buffers: ") + cudaGetErrorString(e); free_blocks(h); return CX_ERR_NOMEM; }
+      h->bufs.push_back(p);
+    }
+    void* u = nullptr;
+    if (cudaMalloc(&u, N * sizeof(double2)) != cudaSuccess) { h->err = "cx_set_blocks: bound vectors"; free_blocks(h); return CX_ERR_NOMEM; }
+    cudaMemset(u, 0, N * sizeof(double2));
+    h->ubgv.push_back(u);
+  }
+  h->psi_sel.assign(1, 0);
+  cx_status s;
+  if ((s = dalloc(h, &h->d_state_tab, tab.size())) != CX_OK) { free_blocks(h); return s; }
+  CX_TRY_CUDA(h, cudaMemcpy(h->d_state_tab, tab.data(), sizeof(int2) * tab.size(), cudaMemcpyHostToDevice));
+  const int nseg = std::max(1, h->nl.nseg);
+  {
+    void* p = nullptr;
+    if (cudaMalloc(&p, (size_t)h->nstates * nseg * kAngMax * cs) != cudaSuccess) { h->err = "cx_set_blocks: projector coefficients"; free_blocks(h); return CX_ERR_NOMEM; }
+    h->d_cprime = p;
+  }
+  std::vector<double2> ph;
+  for (int b = 0; b < nblk; ++b) {
+    std::vector<double2> p = segment_phases(h, blocks[b]);
+    if (p.empty()) p.push_back(make_double2(1, 0));
+    ph.insert(ph.end(), p.begin(), p.end());
+  }
+  if ((s = dalloc(h, &h->d_seg_phase, ph.size())) != CX_OK) { free_blocks(h); return s; }
+  CX_TRY_CUDA(h, cudaMemcpy(h->d_seg_phase, ph.data(), sizeof(double2) * ph.size(), cudaMemcpyHostToDevice));
+  h->nl.seg_phase = h->d_seg_phase;
+  std::vector<int> ids(nblk);
+  for (int b = 0; b < nblk; ++b) ids[b] = b;
+  if (prec == CX_PREC_FP64) {
+    std::vector<cplx<double>*> p0, p1;
+    for (int b = 0; b < nblk; ++b) { p0.push_back((cplx<double>*)h->bufs[2 * b]); p1.push_back((cplx<double>*)h->bufs[2 * b + 1]); }
+    std::vector<BlockDev<double>> bd;
+    make_block_devs<double>(h, p0, p1, ids, bd);
+    BlockDev<double>* d = nullptr;
+    if ((s = dalloc(h, &d, bd.size())) != CX_OK) { free_blocks(h); return s; }
+    CX_TRY_CUDA(h, cudaMemcpy(d, bd.data(), sizeof(bd[0]) * bd.size(), cudaMemcpyHostToDevice));
+    h->d_blocks = d;
+  } else {
+    std::vector<cplx<float>*> p0, p1;
+    for (int b = 0; b < nblk; ++b) { p0.push_back((cplx<float>*)h->bufs[2 * b]); p1.push_back((cplx<float>*)h->bufs[2 * b + 1]); }
+    std::vector<BlockDev<float>> bd;
+    make_block_devs<float>(h, p0, p1, ids, bd);
+    BlockDev<float>* d = nullptr;
+    if ((s = dalloc(h, &d, bd.size())) != CX_OK) { free_blocks(h); return s; }
+    CX_TRY_CUDA(h, cudaMemcpy(d, bd.data(), sizeof(bd[0]) * bd.size(), cudaMemcpyHostToDevice));
+    h->d_blocks = d;
+  }
+  return CX_OK;
+}
+
+cx_status cx_set_psi(cx_handle h, int32_t blk, const double* psi) {
+  if (!h || !psi) return CX_ERR_ARG;
+  if (blk < 0 || blk >= h->nblk) { h->err = "cx_set_psi: block index out of range"; return CX_ERR_ARG; }
+  const size_t n = (size_t)h->g.N * h->blocks[blk].Ns;
+  void* dst = h->bufs[2 * blk + h->psi_sel[0]];
+  return cx_host_to_dev(h, psi, dst, n, h->prec);
+}
+
+cx_status cx_get_psi(cx_handle h, int32_t blk, double* psi) {
+  if (!h || !psi) return CX_ERR_ARG;
+  if (blk < 0 || blk >= h->nblk) { h->err = "cx_get_psi: block index out of range"; return CX_ERR_ARG; }
+  const size_t n = (size_t)h->g.N * h->blocks[blk].Ns;
+  const void* src = h->bufs[2 * blk + h->psi_sel[0]];
+  return cx_dev_to_host(h, src, psi, n, h->prec);
+}
+
+cx_status cx_hpsi(cx_handle h, int32_t blk, int32_t ncol, const double* X, double* Y, int32_t prec) {
+  if (!h || !X || !Y) return CX_ERR_ARG;
+  if (blk < 0 || blk >= h->nblk) { h->err = "cx_hpsi: block index out of range (call cx_set_blocks first)"; return CX_ERR_STATE; }
+  if (ncol < 1 || ncol > 65535) { h->err = "cx_hpsi: ncol must be in 1..65535"; return CX_ERR_ARG; }
+  if (prec == CX_PREC_FP64) return hpsi_T<double>(h, blk, ncol, X, Y);
+  if (prec == CX_PREC_MIXED) return hpsi_T<float>(h, blk, ncol, X, Y);
+  h->err = "cx_hpsi: bad prec";
+  return CX_ERR_ARG;
+}
+
+cx_status cx_chebyshev_filter(cx_handle h, int32_t blk, int32_t ncol, const double* X, double* Y, int32_t m, double a, double b,
+                              double a0, int32_t prec) {
+  if (!h || !X || !Y) return CX_ERR_ARG;
+  if (blk < 0 || blk >= h->nblk) { h->err = "cx_chebyshev_filter: block index out of range (call cx_set_blocks first)"; return CX_ERR_STATE; }
+  if (ncol < 1 || ncol > 65535 || m < 1) { h->err = "cx_chebyshev_filter: need 1 <= ncol <= 65535 and m >= 1"; return CX_ERR_ARG; }
+  if (!(b > a) || !(a > a0)) { h->err = "cx_chebyshev_filter: need a0 < a < b (lower bound < cutoff < upper bound)"; return CX_ERR_ARG; }
+  if (prec == CX_PREC_FP64) return filter_T<double>(h, blk, ncol, X, Y, m, a, b, a0);
+  if (prec == CX_PREC_MIXED) return filter_T<float>(h, blk, ncol, X, Y, m, a, b, a0);
+  h->err = "cx_chebyshev_filter: bad prec";
+  return CX_ERR_ARG;
+}
+
+cx_status cx_sync(cx_handle h) {
+  if (!h) return CX_ERR_ARG;
+  CX_TRY_CUDA(h, cudaStreamSynchronize(h->stream));
+  return CX_OK;
+}
+
+cx_status cx_timer_start(cx_handle h) {
+  if (!h) return CX_ERR_ARG;
+  CX_TRY_CUDA(h, cudaEventRecord(h->tev0, h->stream));
+  return CX_OK;
+}
+
+cx_status cx_timer_stop(cx_handle h, double* ms) {
+  if (!h || !ms) return CX_ERR_ARG;
+  CX_TRY_CUDA(h, cudaEventRecord(h->tev1, h->stream));
+  CX_TRY_CUDA(h, cudaEventSynchronize(h->tev1));
+  float f = 0;
+  CX_TRY_CUDA(h, cudaEventElapsedTime(&f, h->tev0, h->tev1));
+  *ms = f;
+  return CX_OK;
+}
+
+cx_status cx_profile_stencil(cx_handle h, int32_t enable) {
+  if (!h) return CX_ERR_ARG;
+  h->prof = enable != 0;
+  h->prof_launches = 0;
+  h->prof_ms = 0;
+  h->prof_bytes = 0;
+  return CX_OK;
+}
+
+cx_status cx_profile_read(cx_handle h, int64_t* launches, double* total_ms, double* bytes) {
+  if (!h) return CX_ERR_ARG;
+  if (launches) *launches = h->prof_launches;
+  if (total_ms) *total_ms = h->prof_ms;
+  if (bytes) *bytes = h->prof_bytes;
+  return CX_OK;
+}
+
+cx_status cx_launch_count(cx_handle h, int64_t* count, int32_t reset) {
+  if (!h) return CX_ERR_ARG;
+  if (count) *count = h->launches;
+  if (reset) h->launches = 0;
+  return CX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,29 @@
+// Host-side helpers shared by the translation units of libcyclix_gpu.so.
+#pragma once
+#include <vector>
+
+#include "cx_internal.h"
+
+// host complex128 (interleaved) <-> device buffer in the given precision
+cx_status cx_host_to_dev(cx_handle h, const double* host, void* dev, size_t n_complex, int prec);
+cx_status cx_dev_to_host(cx_handle h, const void* dev, double* host, size_t n_complex, int prec);
+// releases the workspaces owned by cx_linalg.cu / cx_poisson.cu
+void cx_free_extra(cx_handle h);
+
+namespace cx {
+
+template <typename R>
+cx_status make_block_devs(cx_handle h, const std::vector<cplx<R>*>& b0, const std::vector<cplx<R>*>& b1,
+                          const std::vector<int>& blk_ids, std::vector<BlockDev<R>>& out);
+std::vector<double2> segment_phases(cx_handle h, const cx_block& B);
+void cheb_scalars(int m, double a, double b, double a0, std::vector<StepScalars>& out, int stride, int col);
+
+template <typename R>
+cx_status fused_step(cx_handle h, const BlockDev<R>* d_blocks, const StepScalars* d_scal, int nblk, const int2* d_state_tab,
+                     int nstates, int in_sel, bool use_xprev, cplx<R>* cprime, bool nonlocal, double bytes);
+template <typename R>
+cx_status filter_blocks(cx_handle h, const BlockDev<R>* d_blocks, int nblk, const int2* d_state_tab, int nstates,
+                        size_t total_elems, int sel0, int m, const std::vector<double>& a, const std::vector<double>& b,
+                        const std::vector<double>& a0, cplx<R>* cprime, int* sel_out);
+
+}  // namespace cx

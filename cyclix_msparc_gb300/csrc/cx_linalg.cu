@@ -1,0 +1,604 @@
+// Subspace part of the CheFSI step (src/eigSolver.m:47-124) and host <-> device transfers.
+//
+//  * spectral bounds: a batched Lanczos iteration in the W inner product (the operator is
+//    self-adjoint in it away from the two radial end rows), the extreme Ritz values of the
+//    tridiagonal matrix found by Sturm-sequence bisection on the GPU; it stands in for
+//    eigs(Hfun,N,1,'lr'/'sr') of src/eigSolver.m:47-67 (bup = 1.01 lambda_max, a0 = lambda_min - 0.1);
+//  * Rayleigh-Ritz per block: Gram G = X^H X and M = X^H (H X) (cuBLAS; complex128, or complex64
+//    with 3xBF16 tensor-core emulation and FP32 accumulation), FP64 Cholesky G = R^H R, projected
+//    Hs = R^-H M R^-1 (the orth + psi'*H*psi of :99-104 in a basis of the same span), the general
+//    FP64 eigensolver (:110), real part and ascending sort (:111-116), rotation psi = X R^-1 Q
+//    (:119) and W-normalisation of the columns (:122-124).
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <numeric>
+
+#include "cx_common.h"
+
+namespace cx {
+
+__global__ void k_d2f(const double2* __restrict__ a, float2* __restrict__ b, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    b[i] = make_float2((float)a[i].x, (float)a[i].y);
+}
+__global__ void k_f2d(const float2* __restrict__ a, double2* __restrict__ b, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    b[i] = make_double2((double)a[i].x, (double)a[i].y);
+}
+
+static unsigned grid_for(size_t n) { return (unsigned)std::min<size_t>((n + 255) / 256, 152 * 16); }
+
+static cx_status ensure(cx_handle h, void** p, size_t* cap, size_t bytes) {
+  if (*cap >= bytes) return CX_OK;
+  cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    h->err = std::string("workspace allocation of ") + std::to_string(bytes) + " B: " + cudaGetErrorString(e);
+    return CX_ERR_NOMEM;
+  }
+  *cap = bytes;
+  return CX_OK;
+}
+
+// ------------------------------------------------------------------ W-normalisation (:122-124)
+template <typename R>
+__global__ void k_colnorm_w(const cplx<R>* __restrict__ X, const double* __restrict__ W, int N, double* __restrict__ out) {
+  const cplx<R>* x = X + (size_t)blockIdx.x * N;
+  double acc = 0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const cplx<R> v = x[i];
+    acc += W[i] * ((double)v.x * v.x + (double)v.y * v.y);
+  }
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += red[k];
+    out[blockIdx.x] = 1.0 / sqrt(s);
+  }
+}
+template <typename R>
+__global__ void k_colscale(cplx<R>* __restrict__ X, int N, int ncol, const double* __restrict__ sc) {
+  const size_t n = (size_t)N * ncol;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const R s = (R)sc[i / N];
+    X[i].x *= s;
+    X[i].y *= s;
+  }
+}
+
+// gather columns: out[:, j] = in[:, perm[j]]
+__global__ void k_gather_cols(const double2* __restrict__ in, double2* __restrict__ out, int n, const int* __restrict__ perm) {
+  const size_t tot = (size_t)n * n;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t j = i / n, r = i % n;
+    out[i] = in[(size_t)perm[j] * n + r];
+  }
+}
+
+// ------------------------------------------------------------------ batched Lanczos (W inner product)
+// Per block b the vectors live at v + b*N etc.; scalars alpha[j*nblk+b], beta2[j*nblk+b].
+__device__ __forceinline__ uint32_t hash32(uint32_t x) {
+  x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
+  return x;
+}
+template <typename R>
+__global__ void k_lz_init(cplx<R>* v, cplx<R>* vprev, int N, int nblk, uint32_t seed) {
+  const size_t tot = (size_t)N * nblk;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t b = (uint32_t)(i / N);
+    const uint32_t u = hash32((uint32_t)(i % N) * 2654435761u ^ hash32(seed + 7919u * (b + 1)));
+    v[i].x = (R)((u >> 8) * (1.0 / 16777216.0));
+    v[i].y = 0;
+    vprev[i].x = 0;
+    vprev[i].y = 0;
+  }
+}
+// acc[b] += sum_n W_n Re(conj(a_n) b_n)
+template <typename R>
+__global__ void k_lz_dot(const cplx<R>* __restrict__ a, const cplx<R>* __restrict__ bv, const double* __restrict__ W, int N,
+                         double* __restrict__ acc) {
+  const int b = blockIdx.y;
+  const cplx<R>* x = a + (size_t)b * N;
+  const cplx<R>* y = bv + (size_t)b * N;
+  double s = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x)
+    s += W[i] * ((double)x[i].x * y[i].x + (double)x[i].y * y[i].y);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ double red[32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+    atomicAdd(acc + b, t);
+  }
+}
+// w = w - alpha v - beta vprev ; beta2_next += ||w||_W^2
+template <typename R>
+__global__ void k_lz_update(cplx<R>* __restrict__ w, const cplx<R>* __restrict__ v, const cplx<R>* __restrict__ vprev,
+                            const double* __restrict__ W, int N, const double* __restrict__ alpha, const double* __restrict__ beta2,
+                            double* __restrict__ beta2_next) {
+  const int b = blockIdx.y;
+  const double al = alpha[b];
+  const double be = beta2 ? sqrt(fmax(beta2[b], 0.0)) : 0.0;
+  cplx<R>* x = w + (size_t)b * N;
+  const cplx<R>* v0 = v + (size_t)b * N;
+  const cplx<R>* v1 = vprev + (size_t)b * N;
+  double s = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    cplx<R> t = x[i];
+    t.x = (R)((double)t.x - al * v0[i].x - be * v1[i].x);
+    t.y = (R)((double)t.y - al * v0[i].y - be * v1[i].y);
+    x[i] = t;
+    s += W[i] * ((double)t.x * t.x + (double)t.y * t.y);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ double red[32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+    atomicAdd(beta2_next + b, t);
+  }
+}
+// vprev = v ; v = w / sqrt(beta2) (zero when the iteration broke down)
+template <typename R>
+__global__ void k_lz_shift(const cplx<R>* __restrict__ w, cplx<R>* __restrict__ v, cplx<R>* __restrict__ vprev, int N,
+                           const double* __restrict__ beta2) {
+  const int b = blockIdx.y;
+  const double bb = beta2[b];
+  const double inv = bb > 1e-200 ? 1.0 / sqrt(bb) : 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    const size_t k = (size_t)b * N + i;
+    vprev[k] = v[k];
+    cplx<R> t = w[k];
+    t.x = (R)(t.x * inv);
+    t.y = (R)(t.y * inv);
+    v[k] = t;
+  }
+}
+// normalise the start vectors: v /= ||v||_W
+template <typename R>
+__global__ void k_lz_norm0(cplx<R>* __restrict__ v, int N, const double* __restrict__ n2) {
+  const int b = blockIdx.y;
+  const double inv = 1.0 / sqrt(n2[b]);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    const size_t k = (size_t)b * N + i;
+    v[k].x = (R)(v[k].x * inv);
+    v[k].y = (R)(v[k].y * inv);
+  }
+}
+// Extreme eigenvalues of the K x K Lanczos tridiagonal of each block by Sturm bisection.
+__device__ int sturm_count(const double* a, const double* b2, int K, int nblk, int blk, double x) {
+  int cnt = 0;
+  double d = 1.0;
+  for (int j = 0; j < K; ++j) {
+    const double off = j == 0 ? 0.0 : b2[(size_t)j * nblk + blk] / d;
+    d = a[(size_t)j * nblk + blk] - x - off;
+    if (fabs(d) < 1e-300) d = -1e-300;
+    if (d < 0) ++cnt;
+  }
+  return cnt;
+}
+__global__ void k_tridiag_extremes(const double* __restrict__ alpha, const double* __restrict__ beta2, int K, int nblk,
+                                   double* __restrict__ lmin, double* __restrict__ lmax) {
+  const int blk = blockIdx.x * blockDim.x + threadIdx.x;
+  if (blk >= nblk) return;
+  // effective length: stop at a breakdown (beta ~ 0)
+  int Ke = K;
+  for (int j = 1; j < K; ++j)
+    if (!(beta2[(size_t)j * nblk + blk] > 1e-24)) { Ke = j; break; }
+  double lo = 1e300, hi = -1e300;
+  for (int j = 0; j < Ke; ++j) {
+    const double a = alpha[(size_t)j * nblk + blk];
+    const double bl = j > 0 ? sqrt(beta2[(size_t)j * nblk + blk]) : 0.0;
+    const double br = j + 1 < Ke ? sqrt(beta2[(size_t)(j + 1) * nblk + blk]) : 0.0;
+    lo = fmin(lo, a - bl - br);
+    hi = fmax(hi, a + bl + br);
+  }
+  // smallest: the least x with count(x) >= 1 ; largest: least x with count(x) >= Ke
+  double l = lo, u = hi;
+  for (int it = 0; it < 200 && u - l > 1e-13 * fmax(1.0, fabs(u) + fabs(l)); ++it) {
+    const double m = 0.5 * (l + u);
+    if (sturm_count(alpha, beta2, Ke, nblk, blk, m) >= 1) u = m; else l = m;
+  }
+  lmin[blk] = 0.5 * (l + u);
+  l = lo; u = hi;
+  for (int it = 0; it < 200 && u - l > 1e-13 * fmax(1.0, fabs(u) + fabs(l)); ++it) {
+    const double m = 0.5 * (l + u);
+    if (sturm_count(alpha, beta2, Ke, nblk, blk, m) >= Ke) u = m; else l = m;
+  }
+  lmax[blk] = 0.5 * (l + u);
+}
+
+// Batched Lanczos over all blocks: fills lmin/lmax (host, nblk each).
+template <typename R>
+static cx_status lanczos_bounds(cx_handle h, int K, std::vector<double>& lmin, std::vector<double>& lmax) {
+  const int nblk = h->nblk, N = h->g.N;
+  const size_t vec = (size_t)N * nblk * sizeof(cplx<R>);
+  const int nseg = std::max(1, h->nl.nseg);
+  const size_t cpb = (size_t)nblk * nseg * kAngMax * sizeof(cplx<R>);
+  const size_t sc = (size_t)(2 * (K + 1) * nblk + 2 * nblk) * sizeof(double);
+  const size_t need = 3 * vec + cpb + sc + nblk * sizeof(BlockDev<R>) + nblk * sizeof(int2) + sizeof(StepScalars) * nblk + 1024;
+  cx_status s = ensure(h, &h->d_lz, &h->lz_bytes, need);
+  if (s != CX_OK) return s;
+  char* p = (char*)h->d_lz;
+  cplx<R>* v = (cplx<R>*)p; p += vec;
+  cplx<R>* w = (cplx<R>*)p; p += vec;
+  cplx<R>* vprev = (cplx<R>*)p; p += vec;
+  cplx<R>* cprime = (cplx<R>*)p; p += cpb;
+  double* alpha = (double*)p; p += (size_t)(K + 1) * nblk * sizeof(double);
+  double* beta2 = (double*)p; p += (size_t)(K + 1) * nblk * sizeof(double);
+  double* dmin = (double*)p; p += nblk * sizeof(double);
+  double* dmax = (double*)p; p += nblk * sizeof(double);
+  p = (char*)(((uintptr_t)p + 255) & ~(uintptr_t)255);
+  BlockDev<R>* d_blk = (BlockDev<R>*)p; p += nblk * sizeof(BlockDev<R>);
+  int2* d_tab = (int2*)p; p += nblk * sizeof(int2);
+  StepScalars* d_sc = (StepScalars*)p;
+
+  std::vector<cplx<R>*> p0(nblk), p1(nblk);
+  std::vector<int> ids(nblk);
+  std::vector<int2> tab(nblk);
+  for (int b = 0; b < nblk; ++b) { p0[b] = v + (size_t)b * N; p1[b] = w + (size_t)b * N; ids[b] = b; tab[b] = make_int2(b, 0); }
+  std::vector<BlockDev<R>> bd;
+  make_block_devs<R>(h, p0, p1, ids, bd);
+  for (auto& d : bd) d.Ns = 1;
+  std::vector<StepScalars> one(nblk, StepScalars{1.0, 0.0, 0.0, 0.0});
+  CX_TRY_CUDA(h, cudaMemcpyAsync(d_blk, bd.data(), nblk * sizeof(BlockDev<R>), cudaMemcpyHostToDevice, h->stream));
+  CX_TRY_CUDA(h, cudaMemcpyAsync(d_tab, tab.data(), nblk * sizeof(int2), cudaMemcpyHostToDevice, h->stream));
+  CX_TRY_CUDA(h, cudaMemcpyAsync(d_sc, one.data(), nblk * sizeof(StepScalars), cudaMemcpyHostToDevice, h->stream));
+  CX_TRY_CUDA(h, cudaMemsetAsync(alpha, 0, 2 * (K + 1) * nblk * sizeof(double), h->stream));
+
+  const dim3 rg((unsigned)std::min(64, (N + 255) / 256), (unsigned)nblk);
+  k_lz_init<R><<<grid_for((size_t)N * nblk), 256, 0, h->stream>>>(v, vprev, N, nblk, 12345u);
+  // ||v0||_W^2 into beta2 row K (scratch), then normalise
+  k_lz_dot<R><<<rg, 256, 0, h->stream>>>(v, v, h->d_W, N, beta2 + (size_t)K * nblk);
+  k_lz_norm0<R><<<rg, 256, 0, h->stream>>>(v, N, beta2 + (size_t)K * nblk);
+  h->launches += 3;
+  for (int j = 0; j < K; ++j) {
+    // w = H v
+    cx_status st = fused_step<R>(h, d_blk, d_sc, nblk, d_tab, nblk, 0, false, cprime, true, 0.0);
+    if (st != CX_OK) return st;
+    k_lz_dot<R><<<rg, 256, 0, h->stream>>>(v, w, h->d_W, N, alpha + (size_t)j * nblk);
+    k_lz_update<R><<<rg, 256, 0, h->stream>>>(w, v, vprev, h->d_W, N, alpha + (size_t)j * nblk,
+                                              j > 0 ? beta2 + (size_t)j * nblk : nullptr, beta2 + (size_t)(j + 1) * nblk);
+    k_lz_shift<R><<<rg, 256, 0, h->stream>>>(w, v, vprev, N, beta2 + (size_t)(j + 1) * nblk);
+    h->launches += 3;
+  }
+  CX_TRY_CUDA(h, cudaGetLastError());
+  k_tridiag_extremes<<<(nblk + 63) / 64, 64, 0, h->stream>>>(alpha, beta2, K, nblk, dmin, dmax);
+  h->launches++;
+  lmin.resize(nblk);
+  lmax.resize(nblk);
+  CX_TRY_CUDA(h, cudaMemcpyAsync(lmin.data(), dmin, nblk * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CX_TRY_CUDA(h, cudaMemcpyAsync(lmax.data(), dmax, nblk * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CX_TRY_CUDA(h, cudaStreamSynchronize(h->stream));
+  return CX_OK;
+}
+
+// ------------------------------------------------------------------ Rayleigh-Ritz of one block
+#define CX_TRY_BLAS(h, expr)                                                          \
+  do {                                                                                \
+    cublasStatus_t _s = (expr);                                                       \
+    if (_s != CUBLAS_STATUS_SUCCESS) {                                                \
+      (h)->err = std::string(#expr) + ": cuBLAS status " + std::to_string((int)_s);   \
+      return CX_ERR_LIB;                                                              \
+    }                                                                                 \
+  } while (0)
+#define CX_TRY_SOLVER(h, expr)                                                        \
+  do {                                                                                \
+    cusolverStatus_t _s = (expr);                                                     \
+    if (_s != CUSOLVER_STATUS_SUCCESS) {                                              \
+      (h)->err = std::string(#expr) + ": cuSOLVER status " + std::to_string((int)_s); \
+      return CX_ERR_LIB;                                                              \
+    }                                                                                 \
+  } while (0)
+
+struct RRWork {
+  double2 *G, *Hs, *V, *ev;
+  float2 *Gf, *Mf, *Cf;
+  double* scfac;
+  int* perm;
+  int* info;
+};
+
+static cx_status rr_workspace(cx_handle h, int nmax, int ncolmax, RRWork& w) {
+  const size_t n2 = (size_t)nmax * nmax;
+  const size_t need = n2 * 16 * 3 + nmax * 16 + n2 * 8 * 3 + (size_t)ncolmax * 8 + nmax * 4 + 64 + 16 * 256;
+  cx_status s = ensure(h, &h->d_rr, &h->rr_bytes, need);
+  if (s != CX_OK) return s;
+  char* p = (char*)h->d_rr;
+  auto take = [&](size_t bytes) { char* q = p; p += (bytes + 255) & ~(size_t)255; return (void*)q; };
+  w.G = (double2*)take(n2 * 16);
+  w.Hs = (double2*)take(n2 * 16);
+  w.V = (double2*)take(n2 * 16);
+  w.ev = (double2*)take(nmax * 16);
+  w.Gf = (float2*)take(n2 * 8);
+  w.Mf = (float2*)take(n2 * 8);
+  w.Cf = (float2*)take(n2 * 8);
+  w.scfac = (double*)take((size_t)ncolmax * 8);
+  w.perm = (int*)take(nmax * 4);
+  w.info = (int*)take(64);
+  return CX_OK;
+}
+
+// Gram and projected matrices into w.G (X^H X) and w.Hs (X^H HX), complex128.
+template <typename R>
+static cx_status rr_gemms(cx_handle h, const cplx<R>* X, const cplx<R>* HX, int N, int n, RRWork& w);
+
+template <>
+cx_status rr_gemms<double>(cx_handle h, const double2* X, const double2* HX, int N, int n, RRWork& w) {
+  const cuDoubleComplex one = make_cuDoubleComplex(1, 0), zero = make_cuDoubleComplex(0, 0);
+  CX_TRY_BLAS(h, cublasSetMathMode(h->cublas, CUBLAS_DEFAULT_MATH));
+  CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_C, CUBLAS_OP_N, n, n, N, &one, (const cuDoubleComplex*)X, N,
+                             (const cuDoubleComplex*)X, N, &zero, (cuDoubleComplex*)w.G, n));
+  CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_C, CUBLAS_OP_N, n, n, N, &one, (const cuDoubleComplex*)X, N,
+                             (const cuDoubleComplex*)HX, N, &zero, (cuDoubleComplex*)w.Hs, n));
+  return CX_OK;
+}
+
+template <>
+cx_status rr_gemms<float>(cx_handle h, const float2* X, const float2* HX, int N, int n, RRWork& w) {
+  const cuComplex one = make_cuComplex(1, 0), zero = make_cuComplex(0, 0);
+  CX_TRY_BLAS(h, cublasSetMathMode(h->cublas, CUBLAS_FP32_EMULATED_BF16X9_MATH));
+  CX_TRY_BLAS(h, cublasSetEmulationStrategy(h->cublas, CUBLAS_EMULATION_STRATEGY_EAGER));
+  CX_TRY_BLAS(h, cublasCgemm(h->cublas, CUBLAS_OP_C, CUBLAS_OP_N, n, n, N, &one, (const cuComplex*)X, N, (const cuComplex*)X, N,
+                             &zero, (cuComplex*)w.Gf, n));
+  CX_TRY_BLAS(h, cublasCgemm(h->cublas, CUBLAS_OP_C, CUBLAS_OP_N, n, n, N, &one, (const cuComplex*)X, N, (const cuComplex*)HX, N,
+                             &zero, (cuComplex*)w.Mf, n));
+  const size_t n2 = (size_t)n * n;
+  k_f2d<<<grid_for(n2), 256, 0, h->stream>>>(w.Gf, w.G, n2);
+  k_f2d<<<grid_for(n2), 256, 0, h->stream>>>(w.Mf, w.Hs, n2);
+  h->launches += 2;
+  return CX_OK;
+}
+
+template <typename R>
+static cx_status rr_rotate(cx_handle h, const cplx<R>* X, cplx<R>* out, int N, int n, RRWork& w);
+
+template <>
+cx_status rr_rotate<double>(cx_handle h, const double2* X, double2* out, int N, int n, RRWork& w) {
+  const cuDoubleComplex one = make_cuDoubleComplex(1, 0), zero = make_cuDoubleComplex(0, 0);
+  CX_TRY_BLAS(h, cublasSetMathMode(h->cublas, CUBLAS_DEFAULT_MATH));
+  CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, N, n, n, &one, (const cuDoubleComplex*)X, N,
+                             (const cuDoubleComplex*)w.V, n, &zero, (cuDoubleComplex*)out, N));
+  return CX_OK;
+}
+
+template <>
+cx_status rr_rotate<float>(cx_handle h, const float2* X, float2* out, int N, int n, RRWork& w) {
+  const cuComplex one = make_cuComplex(1, 0), zero = make_cuComplex(0, 0);
+  const size_t n2 = (size_t)n * n;
+  k_d2f<<<grid_for(n2), 256, 0, h->stream>>>(w.V, w.Cf, n2);
+  h->launches++;
+  CX_TRY_BLAS(h, cublasSetMathMode(h->cublas, CUBLAS_FP32_EMULATED_BF16X9_MATH));
+  CX_TRY_BLAS(h, cublasSetEmulationStrategy(h->cublas, CUBLAS_EMULATION_STRATEGY_EAGER));
+  CX_TRY_BLAS(h, cublasCgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, N, n, n, &one, (const cuComplex*)X, N, (const cuComplex*)w.Cf, n,
+                             &zero, (cuComplex*)out, N));
+  return CX_OK;
+}
+
+template <typename R>
+static cx_status rayleigh_ritz_block(cx_handle h, int b, int sel, RRWork& w, double* eig_out) {
+  const int N = h->g.N, n = h->blocks[b].Ns;
+  const cplx<R>* X = (const cplx<R>*)h->bufs[2 * b + sel];
+  cplx<R>* HX = (cplx<R>*)h->bufs[2 * b + (sel ^ 1)];
+  cx_status s = rr_gemms<R>(h, X, HX, N, n, w);
+  if (s != CX_OK) return s;
+  // Cholesky G = R^H R (upper)
+  size_t wsd = 0, wsh = 0;
+  CX_TRY_SOLVER(h, cusolverDnXpotrf_bufferSize(h->cusolver, h->cusolver_params, CUBLAS_FILL_MODE_UPPER, n, CUDA_C_64F, w.G, n,
+                                                CUDA_C_64F, &wsd, &wsh));
+  size_t wsd2 = 0, wsh2 = 0;
+  CX_TRY_SOLVER(h, cusolverDnXgeev_bufferSize(h->cusolver, h->cusolver_params, CUSOLVER_EIG_MODE_NOVECTOR, CUSOLVER_EIG_MODE_VECTOR, n,
+                                               CUDA_C_64F, w.Hs, n, CUDA_C_64F, w.ev, CUDA_C_64F, nullptr, n, CUDA_C_64F, w.V, n,
+                                               CUDA_C_64F, &wsd2, &wsh2));
+  wsd = std::max(wsd, wsd2);
+  wsh = std::max(wsh, wsh2);
+  if ((s = ensure(h, &h->d_ws, &h->ws_bytes, wsd + 256)) != CX_OK) return s;
+  if (h->hws_bytes < wsh + 256) {
+    cudaFreeHost(h->h_ws);
+    h->h_ws = nullptr;
+    h->hws_bytes = 0;
+    CX_TRY_CUDA(h, cudaMallocHost(&h->h_ws, wsh + 256));
+    h->hws_bytes = wsh + 256;
+  }
+  CX_TRY_SOLVER(h, cusolverDnXpotrf(h->cusolver, h->cusolver_params, CUBLAS_FILL_MODE_UPPER, n, CUDA_C_64F, w.G, n, CUDA_C_64F,
+                                     h->d_ws, h->ws_bytes, h->h_ws, h->hws_bytes, w.info));
+  int info = 0;
+  CX_TRY_CUDA(h, cudaMemcpyAsync(&info, w.info, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CX_TRY_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (info != 0) {
+    h->err = "eigensolver: Gram matrix of block " + std::to_string(b) + " not positive definite (potrf info " + std::to_string(info) +
+             "): the filtered block lost rank";
+    return CX_ERR_NOTPD;
+  }
+  const cuDoubleComplex one = make_cuDoubleComplex(1, 0);
+  CX_TRY_BLAS(h, cublasSetMathMode(h->cublas, CUBLAS_DEFAULT_MATH));
+  // Hs = R^-H M R^-1
+  CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT, n, n, &one,
+                             (const cuDoubleComplex*)w.G, n, (cuDoubleComplex*)w.Hs, n));
+  CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
+                             (const cuDoubleComplex*)w.G, n, (cuDoubleComplex*)w.Hs, n));
+  // general eigensolver (eigSolver.m:110 -- Hs is not Hermitian for Cyclix cells)
+  CX_TRY_SOLVER(h, cusolverDnXgeev(h->cusolver, h->cusolver_params, CUSOLVER_EIG_MODE_NOVECTOR, CUSOLVER_EIG_MODE_VECTOR, n, CUDA_C_64F,
+                                    w.Hs, n, CUDA_C_64F, w.ev, CUDA_C_64F, nullptr, n, CUDA_C_64F, w.V, n, CUDA_C_64F, h->d_ws,
+                                    h->ws_bytes, h->h_ws, h->hws_bytes, w.info));
+  std::vector<std::complex<double>> ev(n);
+  CX_TRY_CUDA(h, cudaMemcpyAsync(ev.data(), w.ev, n * 16, cudaMemcpyDeviceToHost, h->stream));
+  CX_TRY_CUDA(h, cudaMemcpyAsync(&info, w.info, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CX_TRY_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (info != 0) {
+    h->err = "eigensolver: geev of block " + std::to_string(b) + " failed (info " + std::to_string(info) + ")";
+    return CX_ERR_LIB;
+  }
+  // real part, ascending sort (eigSolver.m:111-116)
+  std::vector<int> perm(n);
+  std::iota(perm.begin(), perm.end(), 0);
+  std::stable_sort(perm.begin(), perm.end(), [&](int a, int c) { return ev[a].real() < ev[c].real(); });
+  for (int j = 0; j < n; ++j) eig_out[j] = ev[perm[j]].real();
+  CX_TRY_CUDA(h, cudaMemcpyAsync(w.perm, perm.data(), n * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  k_gather_cols<<<grid_for((size_t)n * n), 256, 0, h->stream>>>(w.V, w.Hs, n, w.perm);
+  h->launches++;
+  // C = R^-1 Q  (into w.V)
+  CX_TRY_CUDA(h, cudaMemcpyAsync(w.V, w.Hs, (size_t)n * n * 16, cudaMemcpyDeviceToDevice, h->stream));
+  CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
+                             (const cuDoubleComplex*)w.G, n, (cuDoubleComplex*)w.V, n));
+  // psi = X C  (into the other buffer), then W-normalise (eigSolver.m:119-124)
+  if ((s = rr_rotate<R>(h, X, HX, N, n, w)) != CX_OK) return s;
+  k_colnorm_w<R><<<n, 256, 0, h->stream>>>(HX, h->d_W, N, w.scfac);
+  k_colscale<R><<<grid_for((size_t)N * n), 256, 0, h->stream>>>(HX, N, n, w.scfac);
+  h->launches += 2;
+  CX_TRY_CUDA(h, cudaGetLastError());
+  return CX_OK;
+}
+
+template <typename R>
+static cx_status eigsolver_T(cx_handle h, int count, int npl, int rhoTrigger, double* EigVal, double* a0, double* bup, double* lc) {
+  const int nblk = h->nblk;
+  std::vector<int> off(nblk + 1, 0);
+  for (int b = 0; b < nblk; ++b) off[b + 1] = off[b] + h->blocks[b].Ns;
+  // ---- bounds and cutoff (eigSolver.m:47-94, first relaxation step)
+  if (count == 1) {
+    std::vector<double> lmin, lmax;
+    cx_status s = lanczos_bounds<R>(h, 64, lmin, lmax);
+    if (s != CX_OK) return s;
+    for (int b = 0; b < nblk; ++b) {
+      bup[b] = lmax[b] * 1.01;
+      a0[b] = lmin[b] - 0.1;
+    }
+  } else if (count > rhoTrigger) {
+    for (int b = 0; b < nblk; ++b) a0[b] = *std::min_element(EigVal + off[b], EigVal + off[b + 1]);
+  }
+  std::vector<double> va(nblk), vb(nblk), va0(nblk);
+  for (int b = 0; b < nblk; ++b) {
+    lc[b] = count == 1 ? 0.5 * (bup[b] + a0[b]) : *std::max_element(EigVal + off[b], EigVal + off[b + 1]) + 0.10;
+    va[b] = lc[b];
+    vb[b] = bup[b];
+    va0[b] = a0[b];
+    if (!(vb[b] > va[b]) || !(va[b] > va0[b])) {
+      h->err = "eigensolver: block " + std::to_string(b) + " has inconsistent bounds (need a0 < cutoff < bup)";
+      return CX_ERR_ARG;
+    }
+  }
+  // ---- Chebyshev filter of all blocks in one batched launch per degree
+  size_t tot = 0;
+  for (int b = 0; b < nblk; ++b) tot += (size_t)h->g.N * h->blocks[b].Ns;
+  int sel = 0;
+  cx_status s = filter_blocks<R>(h, (const BlockDev<R>*)h->d_blocks, nblk, h->d_state_tab, h->nstates, tot, h->psi_sel[0], npl, va,
+                                 vb, va0, (cplx<R>*)h->d_cprime, &sel);
+  if (s != CX_OK) return s;
+  // ---- H * X for all blocks (into the other buffer)
+  {
+    std::vector<StepScalars> one(nblk, StepScalars{1.0, 0.0, 0.0, 0.0});
+    CX_TRY_CUDA(h, cudaMemcpyAsync(h->d_scal, one.data(), nblk * sizeof(StepScalars), cudaMemcpyHostToDevice, h->stream));
+    s = fused_step<R>(h, (const BlockDev<R>*)h->d_blocks, h->d_scal, nblk, h->d_state_tab, h->nstates, sel, false,
+                      (cplx<R>*)h->d_cprime, true, 2.0 * tot * sizeof(cplx<R>));
+    if (s != CX_OK) return s;
+  }
+  // ---- Rayleigh-Ritz per block
+  int nmax = 0;
+  for (int b = 0; b < nblk; ++b) nmax = std::max(nmax, h->blocks[b].Ns);
+  RRWork w{};
+  if ((s = rr_workspace(h, nmax, nmax, w)) != CX_OK) return s;
+  for (int b = 0; b < nblk; ++b) {
+    if ((s = rayleigh_ritz_block<R>(h, b, sel, w, EigVal + off[b])) != CX_OK) return s;
+  }
+  h->psi_sel[0] = sel ^ 1;
+  CX_TRY_CUDA(h, cudaStreamSynchronize(h->stream));
+  return CX_OK;
+}
+
+}  // namespace cx
+
+using namespace cx;
+
+cx_status cx_host_to_dev(cx_handle h, const double* host, void* dev, size_t n, int prec) {
+  if (prec == CX_PREC_FP64) {
+    CX_TRY_CUDA(h, cudaMemcpyAsync(dev, host, n * 16, cudaMemcpyHostToDevice, h->stream));
+    CX_TRY_CUDA(h, cudaStreamSynchronize(h->stream));
+    return CX_OK;
+  }
+  const size_t chunk = std::min<size_t>(n, (size_t)1 << 23);   // 128 MiB of complex128 per pass
+  cx_status s = ensure(h, &h->d_stage, &h->stage_bytes, chunk * 16);
+  if (s != CX_OK) return s;
+  for (size_t o = 0; o < n; o += chunk) {
+    const size_t m = std::min(chunk, n - o);
+    CX_TRY_CUDA(h, cudaMemcpyAsync(h->d_stage, host + 2 * o, m * 16, cudaMemcpyHostToDevice, h->stream));
+    k_d2f<<<grid_for(m), 256, 0, h->stream>>>((const double2*)h->d_stage, (float2*)dev + o, m);
+    h->launches++;
+  }
+  CX_TRY_CUDA(h, cudaGetLastError());
+  CX_TRY_CUDA(h, cudaStreamSynchronize(h->stream));
+  return CX_OK;
+}
+
+cx_status cx_dev_to_host(cx_handle h, const void* dev, double* host, size_t n, int prec) {
+  if (prec == CX_PREC_FP64) {
+    CX_TRY_CUDA(h, cudaMemcpyAsync(host, dev, n * 16, cudaMemcpyDeviceToHost, h->stream));
+    CX_TRY_CUDA(h, cudaStreamSynchronize(h->stream));
+    return CX_OK;
+  }
+  const size_t chunk = std::min<size_t>(n, (size_t)1 << 23);
+  cx_status s = ensure(h, &h->d_stage, &h->stage_bytes, chunk * 16);
+  if (s != CX_OK) return s;
+  for (size_t o = 0; o < n; o += chunk) {
+    const size_t m = std::min(chunk, n - o);
+    k_f2d<<<grid_for(m), 256, 0, h->stream>>>((const float2*)dev + o, (double2*)h->d_stage, m);
+    h->launches++;
+    CX_TRY_CUDA(h, cudaMemcpyAsync(host + 2 * o, h->d_stage, m * 16, cudaMemcpyDeviceToHost, h->stream));
+  }
+  CX_TRY_CUDA(h, cudaGetLastError());
+  CX_TRY_CUDA(h, cudaStreamSynchronize(h->stream));
+  return CX_OK;
+}
+
+void cx_free_extra(cx_handle h) {
+  cudaFree(h->d_stage); h->d_stage = nullptr;
+  cudaFree(h->d_rr); h->d_rr = nullptr;
+  cudaFree(h->d_lz); h->d_lz = nullptr;
+  cudaFree(h->d_misc); h->d_misc = nullptr;
+  cudaFree(h->d_pois); h->d_pois = nullptr;
+}
+
+extern "C" {
+
+cx_status cx_eigsolver(cx_handle h, int32_t count, int32_t npl, int32_t rhoTrigger, double* EigVal, double* a0, double* bup,
+                       double* lambda_cutoff) {
+  if (!h || !EigVal || !a0 || !bup || !lambda_cutoff) return CX_ERR_ARG;
+  if (h->nblk < 1) { h->err = "cx_eigsolver: call cx_set_blocks first"; return CX_ERR_STATE; }
+  if (count < 1 || npl < 1) { h->err = "cx_eigsolver: need count >= 1 and npl >= 1"; return CX_ERR_ARG; }
+  if (h->prec == CX_PREC_FP64) return eigsolver_T<double>(h, count, npl, rhoTrigger, EigVal, a0, bup, lambda_cutoff);
+  return eigsolver_T<float>(h, count, npl, rhoTrigger, EigVal, a0, bup, lambda_cutoff);
+}
+
+cx_status cx_eigsolver_host(cx_handle h, int32_t count, int32_t npl, int32_t rhoTrigger, double* psi, double* EigVal, double* a0,
+                            double* bup, double* lambda_cutoff) {
+  if (!h || !psi) return CX_ERR_ARG;
+  if (h->nblk < 1) { h->err = "cx_eigsolver_host: call cx_set_blocks first"; return CX_ERR_STATE; }
+  size_t off = 0;
+  for (int b = 0; b < h->nblk; ++b) {
+    cx_status s = cx_set_psi(h, b, psi + 2 * off);
+    if (s != CX_OK) return s;
+    off += (size_t)h->g.N * h->blocks[b].Ns;
+  }
+  cx_status s = cx_eigsolver(h, count, npl, rhoTrigger, EigVal, a0, bup, lambda_cutoff);
+  if (s != CX_OK) return s;
+  off = 0;
+  for (int b = 0; b < h->nblk; ++b) {
+    s = cx_get_psi(h, b, psi + 2 * off);
+    if (s != CX_OK) return s;
+    off += (size_t)h->g.N * h->blocks[b].Ns;
+  }
+  return CX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,235 @@
+"""Host-side Cyclix discretisation: the parts of the reference's ``S`` struct that
+the GPU path consumes.
+
+This module builds, with vectorised NumPy, the same quantities that the
+reference computes during initialisation and hands to the Hamiltonian:
+
+* central finite-difference weights ``w1`` / ``w2``
+  (reference: src/initialization.m:403-419);
+* the (r, theta, z) grid with the Dirichlet +1 radial node
+  (src/initialization.m:330-345) and the cyclic / helical cell types
+  (src/initialization.m:286-295);
+* the quadrature weights ``W`` (Cychel/intgWts_cychel.m:1-14);
+* the Bloch wavenumbers of a cyclic / helical cell (integer ``nu`` along
+  theta, Monkhorst-Pack ``eta`` along z, optional time-reversal reduction;
+  src/initialization.m:1591-1682).
+
+The field names follow the reference's struct ``S`` so that a MEX shim, the
+ctypes host mirror and the tests read alike.  Nothing here touches a GPU.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+def fd_weights(FDn: int) -> tuple[np.ndarray, np.ndarray]:
+    """Central FD weights of order 2*FDn for the first and second derivative.
+
+    Returns ``(w1, w2)``, each of length FDn+1, indexed by the offset ``q``
+    (``w[0]`` is the centre).  Closed form of src/initialization.m:403-419:
+    ``w2[k] = 2(-1)^(k+1) (FDn!)^2 / (k^2 (FDn-k)! (FDn+k)!)``,
+    ``w2[0] = -2 sum_k 1/k^2``, ``w1[k] = (-1)^(k+1) (FDn!)^2 / (k (FDn-k)! (FDn+k)!)``.
+    """
+    if FDn < 1:
+        raise ValueError("FDn must be >= 1")
+    f = math.factorial
+    w1 = np.zeros(FDn + 1)
+    w2 = np.zeros(FDn + 1)
+    for k in range(1, FDn + 1):
+        ratio = f(FDn) ** 2 / (f(FDn - k) * f(FDn + k))
+        sgn = 1.0 if (k + 1) % 2 == 0 else -1.0
+        w2[k] = 2.0 * sgn * ratio / (k * k)
+        w2[0] -= 2.0 / (k * k)
+        w1[k] = sgn * ratio / k
+    return w1, w2
+
+
+@dataclass
+class RcImage:
+    """One periodic image of an atom whose projector ball reaches the cell.
+
+    Mirrors ``S.Atom(J).rcImage(img)`` (src/calculate_nloc_projector.m:185-198).
+    ``rc_pos`` holds 1-based linear grid indices, as MATLAB does.
+    """
+    coordinates: np.ndarray          # (3,) image position in (r, theta, z)
+    rc_pos: np.ndarray               # (rc_n_nodes,) int64, 1-based
+    Chi_mat: np.ndarray              # (rc_n_nodes, angnum) float64
+
+    @property
+    def rc_n_nodes(self) -> int:
+        return int(self.rc_pos.shape[0])
+
+
+@dataclass
+class AtomNL:
+    """Nonlocal data of one atom: ``S.Atom(J)`` (src/calculate_nloc_projector.m:252-277)."""
+    angnum: int
+    gamma_Jl: np.ndarray             # (angnum,)
+    rcImage: list = field(default_factory=list)
+
+    @property
+    def n_image_rc(self) -> int:
+        return len(self.rcImage)
+
+
+@dataclass
+class CyclixS:
+    """The subset of the reference struct ``S`` used by the CheFSI path."""
+    Nx: int
+    Ny: int
+    Nz: int
+    FDn: int
+    cell_typ: int
+    BCx: int
+    BCy: int
+    BCz: int
+    dx: float
+    dy: float
+    dz: float
+    xin: float
+    twist: float
+    L1: float
+    L2: float
+    L3: float
+    w1: np.ndarray
+    w2: np.ndarray
+    W: np.ndarray
+    Atoms: np.ndarray                # (n_atm, 3) positions in (r, theta, z)
+    Atom: list                       # list[AtomNL]
+    kptgrid: np.ndarray              # (tnkpt, 3)
+    wkpt: np.ndarray                 # (tnkpt,)
+    nspin: int = 1
+    Nev: int = 0
+    npl: int = 0
+    Veff: np.ndarray | None = None   # (N, nspin)
+    # SCF extras (only the full-SCF workload fills these)
+    b: np.ndarray | None = None
+    rho_at: np.ndarray | None = None
+    NegCharge: float = 0.0
+    Eself: float = 0.0
+    E_corr: float = 0.0
+    bet: float = 0.0
+    elec_T_type: int = 1
+    occfac: float = 2.0
+    n_atm: int = 0
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def N(self) -> int:
+        return self.Nx * self.Ny * self.Nz
+
+    @property
+    def tnkpt(self) -> int:
+        return int(self.kptgrid.shape[0])
+
+    @property
+    def xout(self) -> float:
+        return self.xin + self.L1
+
+
+def cell_type(helical: bool) -> tuple[int, int, int, int]:
+    """(cell_typ, BCx, BCy, BCz) for ``BC: D C P`` (cyclic) or ``D C H`` (cyclic+helical).
+
+    src/initialization.m:286-295: BC 5 -> (3; 1,0,0), BC 7 -> (5; 1,0,0).
+    """
+    return (5, 1, 0, 0) if helical else (3, 1, 0, 0)
+
+
+def radial_nodes(S_or_xin, dx=None, Nx=None) -> np.ndarray:
+    if dx is None:
+        S = S_or_xin
+        return S.xin + np.arange(S.Nx) * S.dx
+    return S_or_xin + np.arange(Nx) * dx
+
+
+def intg_weights(Nx, Ny, Nz, BCy, BCz, xin, dx, dy, dz) -> np.ndarray:
+    """Quadrature weights ``W = kron(Wz, kron(Wy, Wx))`` (Cychel/intgWts_cychel.m:1-14).
+
+    ``Wx = r dx`` with the trapezoid end corrections ``0.5 r dx +- dx^2/8``;
+    ``Wy``, ``Wz`` are ``dy``, ``dz`` halved at Dirichlet ends.
+    """
+    r = xin + np.arange(Nx) * dx
+    Wx = r * dx
+    Wx[0] = 0.5 * xin * dx + 0.125 * dx * dx
+    Wx[Nx - 1] = 0.5 * (xin + (Nx - 1) * dx) * dx - 0.125 * dx * dx
+    Wy = np.full(Ny, dy)
+    Wy[0] *= (1 - BCy * 0.5)
+    Wy[Ny - 1] *= (1 - BCy * 0.5)
+    Wz = np.full(Nz, dz)
+    Wz[0] *= (1 - BCz * 0.5)
+    Wz[Nz - 1] *= (1 - BCz * 0.5)
+    return np.kron(Wz, np.kron(Wy, Wx))
+
+
+def cyclix_kpoints(nkpt, L1, L2, L3, kptshift=(0.0, 0.0, 0.0), time_reversal=True):
+    """Bloch wavenumbers of a cyclic / helical cell (src/initialization.m:1591-1682).
+
+    x: Monkhorst-Pack (ABINIT convention) scaled by 2pi/L1; y (theta): integers
+    ``round((2pi/L2) * (0..n-1)/n)``; z: MP grid shifted by ``kptshift[2]/n`` and
+    mapped into (-1/2, 1/2], scaled by 2pi/L3.  With ``time_reversal`` the
+    reference's pairing rule (sums of x, z equal to 0 and y equal to 0 or
+    2pi/L2) halves the set and doubles the kept weights.
+    Returns ``(kptgrid (tnkpt,3), wkpt (tnkpt,))`` in the reference's ndgrid
+    order (x fastest).
+    """
+    n1, n2, n3 = (int(v) for v in nkpt)
+    eps = np.finfo(float).eps
+
+    def mp1(n):
+        s = -((n - 1) // 2)
+        return np.arange(s, s + n, dtype=float)
+
+    kx = (1.0 / n1) * mp1(n1)
+    ky = (1.0 / n2) * np.arange(n2, dtype=float)
+    kz = (1.0 / n3) * mp1(n3)
+    kz = kz + kptshift[2] * (1.0 / n3)
+    kz = np.mod(kz + 0.5 - eps, 1.0) - 0.5 + eps
+    sumx, sumy, sumz = 0.0, 2 * np.pi / L2, 0.0
+    kx = (2 * np.pi / L1) * kx
+    ky = np.round((2 * np.pi / L2) * ky)
+    kz = (2 * np.pi / L3) * kz
+    KX, KY, KZ = np.meshgrid(kx, ky, kz, indexing="ij")
+    kpt = np.stack([KX.reshape(-1, order="F"), KY.reshape(-1, order="F"), KZ.reshape(-1, order="F")], axis=1)
+    tn = n1 * n2 * n3
+    w = np.ones(tn) / tn
+    if time_reversal:
+        tol = 1e-8
+        drop = np.zeros(tn, bool)
+        dbl = np.zeros(tn, bool)
+        for i in range(tn):
+            for j in range(i + 1, tn):
+                if (abs(kpt[i, 0] + kpt[j, 0] - sumx) < tol
+                        and (abs(kpt[i, 1] + kpt[j, 1] - sumy) < tol or abs(kpt[i, 1] + kpt[j, 1]) < tol)
+                        and abs(kpt[i, 2] + kpt[j, 2] - sumz) < tol):
+                    drop[i] = True
+                    dbl[j] = True
+        w[dbl] *= 2
+        kpt = kpt[~drop]
+        w = w[~drop]
+    return kpt, w
+
+
+def noncart2cart(S, X: np.ndarray) -> np.ndarray:
+    """(r, theta, z) -> Cartesian with the helical twist (Cychel/coordinateTransformation_cychel.m:3-7)."""
+    X = np.atleast_2d(X)
+    ang = X[:, 1] + S.twist * X[:, 2]
+    return np.stack([X[:, 0] * np.cos(ang), X[:, 0] * np.sin(ang), X[:, 2]], axis=1)
+
+
+def rot_z(theta: float) -> np.ndarray:
+    c, s = math.cos(theta), math.sin(theta)
+    return np.array([[c, -s, 0.0], [s, c, 0.0], [0.0, 0.0, 1.0]])
+
+
+def real_ylm(l: int, m: int, X, Y, Z) -> np.ndarray:
+    """Real spherical harmonics for l <= 1 (src/sphericalHarmonics.m:58-80)."""
+    r = np.sqrt(X * X + Y * Y + Z * Z)
+    if l == 0:
+        return 0.282094791773878 * np.ones_like(X)
+    if l == 1:
+        c = 0.488602511902920
+        return c * {-1: Y, 0: Z, 1: X}[m] / r
+    raise ValueError("synthetic projectors use l <= 1")

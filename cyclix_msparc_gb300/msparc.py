@@ -1,0 +1,255 @@
+"""Host mirror of the reference's MATLAB functions on the CheFSI path, backed by libcyclix_gpu.so.
+
+The function names, argument order and meaning follow the reference (paths relative to the
+reference project root ``Cyclix_MS_200220/``):
+
+* ``h_nonlocal_vector_mult(DL11,DL22,DL33,DG1,DG2,DG3,Veff,X,S,kptvec)``  src/h_nonlocal_vector_mult.m:1
+* ``chebyshev_filter(X,m,a,b,a0,DL11,DL22,DL33,DG1,DG2,DG3,Veff,S,kpt_vec)``  src/chebyshev_filter.m:1
+* ``eigSolver(S,count,upper_bound_guess_vecs,psi,EigVal,a0,bup,lambda_cutoff)``  src/eigSolver.m:1
+* ``poissonSolve(S,poisson_tol,Isguess)``  src/poissonSolve.m:1
+
+MATLAB hands the six 1-D operators to the first two; on the GPU the operator is rebuilt from
+the grid in ``S`` and the Bloch vector, so those arguments are accepted and not read.  The GPU
+state (a ``cx_handle``) lives in ``S.gpu`` (see :func:`attach`).  Every failure of the library
+raises :class:`CxError`; nothing falls back to a CPU implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import CxError, check, dptr
+
+__all__ = ["CyclixGPU", "attach", "h_nonlocal_vector_mult", "chebyshev_filter", "eigSolver", "poissonSolve", "CxError"]
+
+
+class CyclixGPU:
+    """Owns one ``cx_handle``: the discretised operator of ``S`` and its Bloch blocks."""
+
+    def __init__(self, S, blocks, prec: str = "mixed"):
+        self.lib = _lib.load()
+        self.S = S
+        self.prec = prec
+        self.N = int(S.Nx * S.Ny * S.Nz)
+        keep = []
+
+        def darr(a):
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            keep.append(a)
+            return dptr(a)
+
+        g = _lib.cx_grid(Nx=S.Nx, Ny=S.Ny, Nz=S.Nz, FDn=S.FDn, cell_typ=S.cell_typ, BCx=S.BCx, BCy=S.BCy, BCz=S.BCz,
+                         dx=S.dx, dy=S.dy, dz=S.dz, xin=S.xin, twist=S.twist, L1=S.L1, L2=S.L2, L3=S.L3,
+                         w1=darr(S.w1), w2=darr(S.w2), W=darr(S.W))
+        atoms = (_lib.cx_atom * max(1, len(S.Atom)))()
+        for J, A in enumerate(S.Atom):
+            imgs = (_lib.cx_rc_image * max(1, A.n_image_rc))()
+            keep.append(imgs)
+            for k, img in enumerate(A.rcImage):
+                pos = np.ascontiguousarray(img.rc_pos, dtype=np.int64)
+                chi = np.asfortranarray(img.Chi_mat, dtype=np.float64)
+                keep.extend([pos, chi])
+                imgs[k].rc_n_nodes = int(pos.shape[0])
+                imgs[k].rc_pos = pos.ctypes.data_as(C.POINTER(C.c_int64))
+                imgs[k].Chi_mat = chi.ctypes.data_as(C.POINTER(C.c_double))
+                for d in range(3):
+                    imgs[k].coordinates[d] = float(img.coordinates[d])
+            atoms[J].angnum = int(A.angnum)
+            atoms[J].n_image_rc = int(A.n_image_rc)
+            atoms[J].gamma_Jl = darr(A.gamma_Jl)
+            for d in range(3):
+                atoms[J].position[d] = float(S.Atoms[J, d])
+            atoms[J].rcImage = C.cast(imgs, C.POINTER(_lib.cx_rc_image))
+        h = C.c_void_p()
+        st = self.lib.cx_create(C.byref(g), len(S.Atom), atoms, int(S.nspin), C.byref(h))
+        if st != _lib.CX_OK:
+            raise CxError(st, self.lib.cx_last_error(None).decode())
+        self.h = h
+        self.set_blocks(blocks, prec)
+        if S.Veff is not None:
+            self.set_veff(S.Veff)
+
+    # -- state -----------------------------------------------------------------------------
+    def set_blocks(self, blocks, prec):
+        self.blocks = [(np.asarray(k, float), int(s), int(n)) for (k, s, n) in blocks]
+        arr = (_lib.cx_block * len(self.blocks))()
+        for i, (k, s, n) in enumerate(self.blocks):
+            for d in range(3):
+                arr[i].kpt_vec[d] = float(k[d])
+            arr[i].spin = s
+            arr[i].Ns = n
+        self.prec = prec
+        check(self.lib, self.h, self.lib.cx_set_blocks(self.h, len(self.blocks), arr, _lib.PREC[prec]))
+        self.Ns = [n for (_, _, n) in self.blocks]
+        self.offsets = np.concatenate([[0], np.cumsum(self.Ns)]).astype(int)
+
+    def set_veff(self, Veff):
+        V = np.asfortranarray(np.asarray(Veff, dtype=np.float64).reshape(self.N, -1, order="F"))
+        check(self.lib, self.h, self.lib.cx_set_veff(self.h, dptr(V)))
+
+    def set_psi(self, blk, psi):
+        a = np.asfortranarray(psi, dtype=np.complex128)
+        assert a.shape == (self.N, self.Ns[blk])
+        check(self.lib, self.h, self.lib.cx_set_psi(self.h, blk, dptr(a.view(np.float64))))
+
+    def get_psi(self, blk):
+        a = np.empty((self.N, self.Ns[blk]), dtype=np.complex128, order="F")
+        check(self.lib, self.h, self.lib.cx_get_psi(self.h, blk, dptr(a.view(np.float64))))
+        return a
+
+    # -- operators ---------------------------------------------------------------------------
+    def hpsi(self, blk, X, prec=None):
+        X = np.asfortranarray(X, dtype=np.complex128)
+        if X.ndim == 1:
+            X = X[:, None]
+        Y = np.empty_like(X, order="F")
+        check(self.lib, self.h, self.lib.cx_hpsi(self.h, blk, X.shape[1], dptr(X.view(np.float64)),
+                                                 dptr(Y.view(np.float64)), _lib.PREC[prec or self.prec]))
+        return Y
+
+    def filter(self, blk, X, m, a, b, a0, prec=None):
+        X = np.asfortranarray(X, dtype=np.complex128)
+        Y = np.empty_like(X, order="F")
+        check(self.lib, self.h, self.lib.cx_chebyshev_filter(self.h, blk, X.shape[1], dptr(X.view(np.float64)),
+                                                             dptr(Y.view(np.float64)), int(m), float(a), float(b), float(a0),
+                                                             _lib.PREC[prec or self.prec]))
+        return Y
+
+    def eigsolve(self, count, npl, EigVal, a0, bup, lambda_cutoff, rhoTrigger=4):
+        """Device-resident eigSolver step: arrays are updated in place."""
+        for v in (EigVal, a0, bup, lambda_cutoff):
+            assert v.dtype == np.float64 and v.flags.c_contiguous
+        check(self.lib, self.h, self.lib.cx_eigsolver(self.h, int(count), int(npl), int(rhoTrigger), dptr(EigVal), dptr(a0),
+                                                      dptr(bup), dptr(lambda_cutoff)))
+
+    def eigsolve_host(self, count, npl, psi_packed, EigVal, a0, bup, lambda_cutoff, rhoTrigger=4):
+        assert psi_packed.dtype == np.complex128 and psi_packed.flags.c_contiguous or psi_packed.flags.f_contiguous
+        check(self.lib, self.h, self.lib.cx_eigsolver_host(self.h, int(count), int(npl), int(rhoTrigger),
+                                                           dptr(psi_packed.reshape(-1, order="A").view(np.float64)),
+                                                           dptr(EigVal), dptr(a0), dptr(bup), dptr(lambda_cutoff)))
+
+    def poisson(self, f, phi0=None, tol=1e-8, maxit=1000):
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        phi = np.ascontiguousarray(phi0 if phi0 is not None else np.zeros(self.N), dtype=np.float64).copy()
+        it = C.c_int32(0)
+        rr = C.c_double(0)
+        st = self.lib.cx_poisson(self.h, dptr(f), dptr(phi), float(tol), int(maxit), 1 if phi0 is not None else 0,
+                                 C.byref(it), C.byref(rr))
+        if st not in (_lib.CX_OK, _lib.CX_ERR_NOCONV):
+            check(self.lib, self.h, st)
+        return phi, int(it.value), float(rr.value), st == _lib.CX_OK
+
+    # -- measurement --------------------------------------------------------------------------
+    def sync(self):
+        check(self.lib, self.h, self.lib.cx_sync(self.h))
+
+    def timer_start(self):
+        check(self.lib, self.h, self.lib.cx_timer_start(self.h))
+
+    def timer_stop(self) -> float:
+        ms = C.c_double(0)
+        check(self.lib, self.h, self.lib.cx_timer_stop(self.h, C.byref(ms)))
+        return ms.value
+
+    def profile(self, enable: bool):
+        check(self.lib, self.h, self.lib.cx_profile_stencil(self.h, 1 if enable else 0))
+
+    def profile_read(self):
+        n = C.c_int64(0)
+        ms = C.c_double(0)
+        by = C.c_double(0)
+        check(self.lib, self.h, self.lib.cx_profile_read(self.h, C.byref(n), C.byref(ms), C.byref(by)))
+        return n.value, ms.value, by.value
+
+    def launch_count(self, reset=False) -> int:
+        n = C.c_int64(0)
+        check(self.lib, self.h, self.lib.cx_launch_count(self.h, C.byref(n), 1 if reset else 0))
+        return n.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.cx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def attach(S, blocks, prec="mixed") -> CyclixGPU:
+    """Create the GPU operator for ``S`` and keep it in ``S.gpu``."""
+    S.gpu = CyclixGPU(S, blocks, prec)
+    return S.gpu
+
+
+def _block_of(S, kptvec, Veff=None):
+    gpu = S.gpu
+    k = np.asarray(kptvec, float)
+    cands = [i for i, (kk, s, n) in enumerate(gpu.blocks) if np.allclose(kk, k, atol=0, rtol=0)]
+    if not cands:
+        raise CxError(_lib.CX_ERR_ARG, "no block with this kptvec; pass it in the block list of attach()")
+    if Veff is not None and len(cands) > 1 and S.Veff is not None:
+        for i in cands:
+            if np.array_equal(np.asarray(S.Veff)[:, gpu.blocks[i][1]], np.asarray(Veff).reshape(-1)):
+                return i
+    return cands[0]
+
+
+def h_nonlocal_vector_mult(DL11, DL22, DL33, DG1, DG2, DG3, Veff, X, S, kptvec):
+    """``Hnlx = (-0.5*Lap + Veff) X + Vnl X`` for the block of ``kptvec`` (src/h_nonlocal_vector_mult.m:1-43)."""
+    blk = _block_of(S, kptvec, Veff)
+    return S.gpu.hpsi(blk, X)
+
+
+def chebyshev_filter(X, m, a, b, a0, DL11, DL22, DL33, DG1, DG2, DG3, Veff, S, kpt_vec):
+    """Scaled Chebyshev filter of degree m (src/chebyshev_filter.m:1-44); a = cutoff, b = upper, a0 = lower."""
+    blk = _block_of(S, kpt_vec, Veff)
+    return S.gpu.filter(blk, X, m, a, b, a0)
+
+
+def eigSolver(S, count, upper_bound_guess_vecs, psi, EigVal, a0, bup, lambda_cutoff):
+    """``[ubgv,psi,EigVal,a0,bup,lambda_cutoff] = eigSolver(S,count,...)`` (src/eigSolver.m:1-125).
+
+    ``psi`` is N x Nev x (tnkpt*nspin) as in MATLAB (or a list of per-block N x Ns arrays for
+    uneven blocks); it is copied to the GPU, updated there and copied back, like a MEX call.
+    """
+    gpu = S.gpu
+    uniform = not isinstance(psi, (list, tuple))
+    blocks = [psi[:, :, k] for k in range(psi.shape[2])] if uniform else list(psi)
+    packed = np.concatenate([np.asarray(b, np.complex128).reshape(-1, order="F") for b in blocks])
+    EV = np.ascontiguousarray(np.concatenate([np.asarray(EigVal)[:gpu.Ns[k], k] for k in range(len(gpu.Ns))])
+                              if uniform and np.ndim(EigVal) == 2 else np.asarray(EigVal, float).reshape(-1), dtype=np.float64)
+    a0 = np.ascontiguousarray(a0, dtype=np.float64).reshape(-1).copy()
+    bup = np.ascontiguousarray(bup, dtype=np.float64).reshape(-1).copy()
+    lc = np.ascontiguousarray(lambda_cutoff, dtype=np.float64).reshape(-1).copy()
+    gpu.eigsolve_host(count, S.npl, packed, EV, a0, bup, lc, rhoTrigger=getattr(S, "rhoTrigger", 4))
+    out = []
+    for k, n in enumerate(gpu.Ns):
+        o = gpu.offsets[k] * gpu.N
+        out.append(packed[o:o + gpu.N * n].reshape(gpu.N, n, order="F"))
+    if uniform:
+        psi_out = np.stack(out, axis=2)
+        EigVal_out = np.stack([EV[gpu.offsets[k]:gpu.offsets[k + 1]] for k in range(len(gpu.Ns))], axis=1)
+    else:
+        psi_out = out
+        EigVal_out = EV
+    return upper_bound_guess_vecs, psi_out, EigVal_out, a0, bup, lc
+
+
+def poissonSolve(S, poisson_tol, Isguess):
+    """``S = poissonSolve(S, poisson_tol, Isguess)`` for Cyclix cells (src/poissonSolve.m:1-51).
+
+    ``f = -4 pi (rho + b)`` (:19-23), AAR with omega = beta = 0.6, m = 7, p = 6 (:36) and
+    ``S.MAXIT_POISSON`` iterations; the converged potential is stored in ``S.phi``.
+    """
+    f = -4 * np.pi * (np.asarray(S.rho).reshape(S.N, -1, order="F")[:, 0] + S.b)
+    guess = S.phi if (Isguess and getattr(S, "phi", None) is not None) else None
+    phi, it, rr, ok = S.gpu.poisson(f, guess, poisson_tol, getattr(S, "MAXIT_POISSON", 1000))
+    S.phi = phi
+    S.extra["poisson_iters"] = it
+    S.extra["poisson_relres"] = rr
+    return S

@@ -1,0 +1,162 @@
+/*
+ * cyclix_gpu.h -- C-ABI of libcyclix_gpu.so, the GB300 (sm_103a) implementation of
+ * Cyclix's Chebyshev-filtered subspace iteration.
+ *
+ * The entry points replace the reference's MATLAB functions on the CheFSI path
+ * (paths relative to the reference project root Cyclix_MS_200220/):
+ *
+ *   cx_hpsi             h_nonlocal_vector_mult(DL11,DL22,DL33,DG1,DG2,DG3,Veff,X,S,kptvec)
+ *                         src/h_nonlocal_vector_mult.m:1 (with lapVec src/lapVec.m:1 ->
+ *                         Cychel/lapVec_cychel.m:1)
+ *   cx_chebyshev_filter chebyshev_filter(X,m,a,b,a0,DL11,...,Veff,S,kpt_vec)
+ *                         src/chebyshev_filter.m:1
+ *   cx_eigsolver        [ubgv,psi,EigVal,a0,bup,lambda_cutoff] = eigSolver(S,count,ubgv,psi,EigVal,a0,bup,lambda_cutoff)
+ *                         src/eigSolver.m:1, called from src/scf.m:123-124
+ *   cx_poisson          S = poissonSolve(S,poisson_tol,Isguess) -> aar(Lap_std,f,...)
+ *                         src/poissonSolve.m:1, src/aar.m:1
+ *
+ * The operator data that MATLAB keeps in the struct S (grid, FD weights,
+ * quadrature weights, KB projector images) is handed over once in cx_create;
+ * the Bloch blocks (k-point, spin, number of states) in cx_set_blocks.
+ *
+ * Conventions
+ *  - Host arrays are MATLAB column-major.  Complex arrays are interleaved
+ *    (re, im) doubles, i.e. the R2018a mxGetComplexDoubles layout.
+ *  - psi of one block is N x Ns, N = Nx*Ny*Nz with x (r) fastest, then y (theta), then z.
+ *  - Every call returns a cx_status; CX_OK is 0.  No call aborts or exits the
+ *    process.  cx_last_error() gives the message of the last failure.
+ *  - One CUDA stream per handle; calls on one handle are not thread-safe.
+ */
+#ifndef CYCLIX_GPU_H
+#define CYCLIX_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t cx_status;
+enum {
+  CX_OK = 0,
+  CX_ERR_ARG = 1,        /* invalid argument (sizes, null pointers, unsupported FD order) */
+  CX_ERR_CUDA = 2,       /* CUDA runtime error */
+  CX_ERR_NOMEM = 3,      /* device allocation failed */
+  CX_ERR_LIB = 4,        /* cuBLAS / cuSOLVER error */
+  CX_ERR_NOTPD = 5,      /* Gram matrix not positive definite (filtered block lost rank) */
+  CX_ERR_STATE = 6,      /* call out of order (e.g. eigensolver before cx_set_blocks) */
+  CX_ERR_NOCONV = 7      /* iterative solver hit its iteration limit */
+};
+
+/* Arithmetic of the filter / subspace path. */
+enum {
+  CX_PREC_FP64 = 0,      /* complex128 everywhere: the plain FP64 path */
+  CX_PREC_MIXED = 1      /* complex64 filter and H*psi, 3xBF16 tensor-core subspace GEMMs with FP32
+                            accumulation, FP64 Cholesky / eigensolver / refinement */
+};
+
+typedef struct cx_handle_s* cx_handle;
+
+/* Grid and discretisation: the S fields that lapIndicesValues_1d_cychel
+ * (Cychel/lapIndicesValues_1d_cychel.m:9-15) and intgWts_cychel read. */
+typedef struct {
+  int32_t Nx, Ny, Nz;        /* nodes (S.Nx etc. after the +BC node) */
+  int32_t FDn;               /* half FD order; 1..8 supported (FD order 12 -> 6) */
+  int32_t cell_typ;          /* 3 cyclic, 4/5 helical */
+  int32_t BCx, BCy, BCz;     /* 1 Dirichlet, 0 periodic; BCx must be 1 (radial walls) */
+  double dx, dy, dz;
+  double xin;                /* inner radius */
+  double twist;              /* S.twist (rad/bohr); 0 for cell_typ 3 */
+  double L1, L2, L3;
+  const double* w1;          /* S.w1, FDn+1 entries (src/initialization.m:413-418) */
+  const double* w2;          /* S.w2, FDn+1 entries (src/initialization.m:404-410) */
+  const double* W;           /* S.W, N quadrature weights (Cychel/intgWts_cychel.m) */
+} cx_grid;
+
+/* S.Atom(J).rcImage(img) (src/calculate_nloc_projector.m:185-198) */
+typedef struct {
+  int32_t rc_n_nodes;
+  const int64_t* rc_pos;     /* 1-based linear grid indices */
+  const double* Chi_mat;     /* rc_n_nodes x angnum, column-major */
+  double coordinates[3];     /* image position (r, theta, z) */
+} cx_rc_image;
+
+/* S.Atom(J) and S.Atoms(J,:) (src/calculate_nloc_projector.m:252-277) */
+typedef struct {
+  int32_t angnum;
+  int32_t n_image_rc;
+  const double* gamma_Jl;    /* angnum */
+  double position[3];        /* S.Atoms(J,:) */
+  const cx_rc_image* rcImage;
+} cx_atom;
+
+/* One (k-point, spin) block: eigSolver's ks (src/eigSolver.m:26-33). */
+typedef struct {
+  double kpt_vec[3];         /* S.kptgrid(kpt,:) */
+  int32_t spin;              /* 0-based spin channel (column of S.Veff) */
+  int32_t Ns;                /* states in this block (S.Nev; may differ per block) */
+} cx_block;
+
+/* ---- lifecycle ---------------------------------------------------------- */
+cx_status cx_create(const cx_grid* grid, int32_t n_atm, const cx_atom* atoms, int32_t nspin, cx_handle* out);
+cx_status cx_destroy(cx_handle h);
+/* Message of the last failed call on h (or of the last failed cx_create when h is NULL). */
+const char* cx_last_error(cx_handle h);
+/* Library version string. */
+const char* cx_version(void);
+
+/* Blocks and working precision; allocates two device buffers per block
+ * (psi and one work array).  Replaces any previous block set. */
+cx_status cx_set_blocks(cx_handle h, int32_t nblk, const cx_block* blocks, int32_t prec);
+/* S.Veff: N x nspin, column-major (src/scf.m:39). */
+cx_status cx_set_veff(cx_handle h, const double* Veff);
+/* Device-resident psi of one block: host N x Ns complex (interleaved). */
+cx_status cx_set_psi(cx_handle h, int32_t blk, const double* psi);
+cx_status cx_get_psi(cx_handle h, int32_t blk, double* psi);
+
+/* ---- the MATLAB functions ---------------------------------------------- */
+/* Hnlx = h_nonlocal_vector_mult(..., Veff, X, S, kptvec) for block blk:
+ * X, Y host N x ncol complex.  prec selects complex128 or complex64 arithmetic. */
+cx_status cx_hpsi(cx_handle h, int32_t blk, int32_t ncol, const double* X, double* Y, int32_t prec);
+
+/* Y = chebyshev_filter(X, m, a, b, a0, ...) for block blk (a = cutoff, b = upper
+ * bound, a0 = lower bound, as the reference names them at src/chebyshev_filter.m:1). */
+cx_status cx_chebyshev_filter(cx_handle h, int32_t blk, int32_t ncol, const double* X, double* Y,
+                              int32_t m, double a, double b, double a0, int32_t prec);
+
+/* The eigSolver step over all blocks on the device-resident psi (src/eigSolver.m:26-125):
+ * spectral bounds when count == 1 (Lanczos), filter cutoff, Chebyshev filter of degree npl,
+ * orthonormalisation, projected Hamiltonian, general FP64 subspace eigensolver, sort,
+ * rotation and W-normalisation.  EigVal is packed: block b's Ns_b values follow block b-1's.
+ * a0, bup, lambda_cutoff have nblk entries each (in/out).  rhoTrigger as src/scf.m:93. */
+cx_status cx_eigsolver(cx_handle h, int32_t count, int32_t npl, int32_t rhoTrigger,
+                       double* EigVal, double* a0, double* bup, double* lambda_cutoff);
+
+/* The same step with host psi in and out (N x Ns_b per block, blocks back to back),
+ * the drop-in for a MEX call that passes S.psi: the copies are part of the call. */
+cx_status cx_eigsolver_host(cx_handle h, int32_t count, int32_t npl, int32_t rhoTrigger, double* psi,
+                            double* EigVal, double* a0, double* bup, double* lambda_cutoff);
+
+/* phi = aar(Lap_std, f, guess, tol, maxit, 0.6, 0.6, 7, 6, ...) (src/poissonSolve.m:36,
+ * src/aar.m:1-74) with f = -4*pi*(rho+b) given; a Jacobi preconditioner replaces ILU.
+ * phi is the initial guess when use_guess != 0 (else ones, as aar.m:51-53) and the result. */
+cx_status cx_poisson(cx_handle h, const double* f, double* phi, double tol, int32_t maxit,
+                     int32_t use_guess, int32_t* iters, double* relres);
+
+/* ---- measurement -------------------------------------------------------- */
+/* Wait for all work of h. */
+cx_status cx_sync(cx_handle h);
+/* CUDA-event timer on the handle's stream. */
+cx_status cx_timer_start(cx_handle h);
+cx_status cx_timer_stop(cx_handle h, double* ms);
+/* Per-kernel device timing of the Chebyshev stencil launches (enable, then read
+ * launches and total ms since enabling). */
+cx_status cx_profile_stencil(cx_handle h, int32_t enable);
+cx_status cx_profile_read(cx_handle h, int64_t* launches, double* total_ms, double* bytes);
+/* Number of this library's kernel launches issued on h since the last reset. */
+cx_status cx_launch_count(cx_handle h, int64_t* count, int32_t reset);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CYCLIX_GPU_H */

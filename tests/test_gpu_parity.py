@@ -1,0 +1,195 @@
+"""GPU parity: libcyclix_gpu.so (through the C-ABI) against the CPU oracle on seeded inputs.
+
+Tolerances (stated per test):
+  * H*psi, filter: max |GPU - oracle| / max |oracle| <= 1e-12 for complex128, <= 2e-6 for complex64;
+  * subspace eigenvalues: <= 1e-9 Ha (complex128), <= 1e-5 Ha (mixed, before the FP64 refinement);
+  * Poisson: relative residual of the GPU potential <= the requested tolerance.
+"""
+import numpy as np
+import pytest
+
+from oracle import cychel_ops as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _blocks(S, Ns):
+    from cyclix_msparc_gb300.workloads import block_layout, Workload
+    out = []
+    ks = 0
+    for spin in range(S.nspin):
+        for k in range(S.tnkpt):
+            out.append((S.kptgrid[k].copy(), spin, int(Ns[ks])))
+            ks += 1
+    return out
+
+
+def _rand(N, n, seed):
+    rng = np.random.default_rng(seed)
+    return np.asfortranarray(rng.standard_normal((N, n)) + 1j * rng.standard_normal((N, n)))
+
+
+def _relerr(a, b):
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+@pytest.fixture(scope="module")
+def gpu_cyclic(small_cyclic):
+    from cyclix_msparc_gb300.msparc import CyclixGPU
+    S = small_cyclic
+    g = CyclixGPU(S, _blocks(S, S.extra["Ns"]), "fp64")
+    yield g
+    g.close()
+
+
+@pytest.fixture(scope="module")
+def gpu_helical(small_helical):
+    from cyclix_msparc_gb300.msparc import CyclixGPU
+    S = small_helical
+    g = CyclixGPU(S, _blocks(S, S.extra["Ns"]), "fp64")
+    yield g
+    g.close()
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("mixed", 2e-6)])
+def test_hpsi_cyclic(small_cyclic, gpu_cyclic, prec, tol):
+    S = small_cyclic
+    X = _rand(S.N, 7, 1)
+    H = O.Hamiltonian(S, S.kptgrid[0], S.Veff[:, 0])
+    ref = H(X)
+    got = gpu_cyclic.hpsi(0, X, prec)
+    assert _relerr(got, ref) < tol
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("mixed", 2e-6)])
+def test_hpsi_helical_all_blocks(small_helical, gpu_helical, prec, tol):
+    S = small_helical
+    for b, (k, spin, n) in enumerate(gpu_helical.blocks):
+        X = _rand(S.N, 3, 10 + b)
+        H = O.Hamiltonian(S, k, S.Veff[:, spin])
+        assert _relerr(gpu_helical.hpsi(b, X, prec), H(X)) < tol, (b, k, spin)
+
+
+def test_hpsi_local_only_matches_assembled_operator(small_cyclic, gpu_cyclic):
+    """Without projectors the operator is -1/2 Lap + Veff with the kron-assembled Lap (initialization.m:735-740)."""
+    S = small_cyclic
+    X = _rand(S.N, 2, 3)
+    L = O.lap_full_k(S, S.kptgrid[0])
+    ref_local = -0.5 * (L @ X) + S.Veff[:, :1] * X
+    H = O.Hamiltonian(S, S.kptgrid[0], S.Veff[:, 0])
+    nl = H(X) - ref_local                      # the oracle's nonlocal part
+    got = gpu_cyclic.hpsi(0, X, "fp64")
+    assert _relerr(got - nl, ref_local) < 1e-12
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-11), ("mixed", 5e-6)])
+def test_chebyshev_filter(small_cyclic, gpu_cyclic, prec, tol):
+    S = small_cyclic
+    H = O.Hamiltonian(S, S.kptgrid[0], S.Veff[:, 0])
+    X = _rand(S.N, 5, 4)
+    a0, bup, cut = -3.5, 800.0, 2.0
+    ref = O.chebyshev_filter(X, 8, cut, bup, a0, H)
+    got = gpu_cyclic.filter(0, X, 8, cut, bup, a0, prec)
+    assert _relerr(got, ref) < tol
+
+
+def test_chebyshev_filter_helical(small_helical, gpu_helical):
+    S = small_helical
+    k, spin, n = gpu_helical.blocks[3]
+    H = O.Hamiltonian(S, k, S.Veff[:, spin])
+    X = _rand(S.N, 4, 5)
+    ref = O.chebyshev_filter(X, 6, 1.0, 300.0, -4.0, H)
+    got = gpu_helical.filter(3, X, 6, 1.0, 300.0, -4.0, "fp64")
+    assert _relerr(got, ref) < 1e-11
+
+
+def _eig_case(S, g, prec, count):
+    """Run one eigSolver step (count > 1 path: bounds given) on GPU and oracle from the same psi."""
+    from cyclix_msparc_gb300.workloads import initial_psi
+    nblk = len(g.blocks)
+    psis = [initial_psi(S.N, n, 100 + b) for b, (_, _, n) in enumerate(g.blocks)]
+    EigPrev = [np.linspace(-2.0, 0.5, n) for (_, _, n) in g.blocks]
+    a0 = np.array([-3.0] * nblk)
+    bup = np.array([900.0] * nblk)
+    lc = np.zeros(nblk)
+    for b in range(nblk):
+        g.set_psi(b, psis[b])
+    EV = np.ascontiguousarray(np.concatenate(EigPrev))
+    g.eigsolve(count, S.npl, EV, a0.copy(), bup.copy(), lc, rhoTrigger=4)
+    out = []
+    for b, (k, spin, n) in enumerate(g.blocks):
+        H = O.Hamiltonian(S, k, S.Veff[:, spin])
+        psi_ref, ev_ref, _ = O.eig_solver_block(S, H, psis[b], count, (a0[b], bup[b], 0.0), EigPrev[b])
+        ev = EV[g.offsets[b]:g.offsets[b + 1]]
+        out.append((ev, ev_ref, g.get_psi(b), psi_ref))
+    return out
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-9), ("mixed", 1e-5)])
+def test_eigsolver_cyclic(small_cyclic, prec, tol):
+    from cyclix_msparc_gb300.msparc import CyclixGPU
+    S = small_cyclic
+    g = CyclixGPU(S, _blocks(S, S.extra["Ns"]), prec)
+    try:
+        for ev, ev_ref, psi, psi_ref in _eig_case(S, g, prec, 2):
+            assert np.max(np.abs(ev - ev_ref)) < tol
+            # W-normalised columns spanning the oracle's Ritz vectors: |<psi_j, psi_ref_j>_W| == 1
+            ov = np.abs(np.sum(S.W[:, None] * np.conj(psi) * psi_ref, axis=0))
+            lowest = slice(0, psi.shape[1] // 2)
+            assert np.max(np.abs(ov[lowest] - 1)) < (1e-7 if prec == "fp64" else 1e-3)
+    finally:
+        g.close()
+
+
+def test_eigsolver_helical_fp64(small_helical):
+    from cyclix_msparc_gb300.msparc import CyclixGPU
+    S = small_helical
+    g = CyclixGPU(S, _blocks(S, S.extra["Ns"]), "fp64")
+    try:
+        for ev, ev_ref, psi, psi_ref in _eig_case(S, g, "fp64", 5):
+            assert np.max(np.abs(ev - ev_ref)) < 1e-9
+    finally:
+        g.close()
+
+
+def test_spectral_bounds_bracket_the_spectrum(tiny_helical):
+    """count == 1: Lanczos bounds must bracket the dense spectrum as eigs' bounds do (eigSolver.m:47-67)."""
+    from cyclix_msparc_gb300.msparc import CyclixGPU
+    from cyclix_msparc_gb300.workloads import initial_psi
+    S = tiny_helical
+    g = CyclixGPU(S, _blocks(S, S.extra["Ns"]), "fp64")
+    try:
+        nblk = len(g.blocks)
+        for b, (_, _, n) in enumerate(g.blocks):
+            g.set_psi(b, initial_psi(S.N, n, b))
+        EV = np.zeros(int(sum(g.Ns)))
+        a0, bup, lc = np.zeros(nblk), np.zeros(nblk), np.zeros(nblk)
+        g.eigsolve(1, S.npl, EV, a0, bup, lc)
+        for b, (k, spin, n) in enumerate(g.blocks):
+            H = O.Hamiltonian(S, k, S.Veff[:, spin])
+            lam = np.linalg.eigvals(H.dense())
+            lmax, lmin = lam.real.max(), lam.real.min()
+            assert bup[b] >= lmax * 1.0 and bup[b] <= lmax * 1.02
+            assert a0[b] <= lmin and a0[b] >= lmin - 0.2
+            assert lc[b] == pytest.approx(0.5 * (bup[b] + a0[b]))
+    finally:
+        g.close()
+
+
+def test_poisson_aar(small_cyclic):
+    import scipy.sparse.linalg as spla
+    from cyclix_msparc_gb300.msparc import CyclixGPU
+    S = small_cyclic
+    g = CyclixGPU(S, _blocks(S, S.extra["Ns"]), "fp64")
+    try:
+        rng = np.random.default_rng(7)
+        rho = np.exp(-((np.arange(S.N) % S.Nx) - S.Nx / 2) ** 2 / 20.0) * (1 + 0.1 * rng.standard_normal(S.N))
+        f = -4 * np.pi * (rho - (S.W @ rho) / S.W.sum())
+        L = O.lap_std(S)
+        phi, it, rr, ok = g.poisson(f, None, 1e-8, 2000)
+        assert ok and rr <= 1e-8
+        assert np.linalg.norm(f - L @ phi) / np.linalg.norm(f) <= 1.01e-8
+        ref = spla.spsolve(L.tocsc(), f)
+        assert np.max(np.abs(phi - ref)) / np.max(np.abs(ref)) < 1e-5
+    finally:
+        g.close()
