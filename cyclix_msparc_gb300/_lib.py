@@ -19,7 +19,8 @@ PREC = {"fp64": CX_PREC_FP64, "mixed": CX_PREC_MIXED}
 
 EXPORTS = ["cx_create", "cx_destroy", "cx_last_error", "cx_version", "cx_set_blocks", "cx_set_veff", "cx_set_psi",
            "cx_get_psi", "cx_hpsi", "cx_chebyshev_filter", "cx_eigsolver", "cx_eigsolver_host", "cx_poisson", "cx_sync",
-           "cx_timer_start", "cx_timer_stop", "cx_profile_stencil", "cx_profile_read", "cx_launch_count"]
+           "cx_timer_start", "cx_timer_stop", "cx_profile_stencil", "cx_profile_read", "cx_launch_count",
+           "cx_host_register", "cx_host_unregister"]
 
 
 class cx_grid(C.Structure):
@@ -82,6 +83,8 @@ def load(build_if_missing: bool = True):
         "cx_profile_stencil": ([h, C.c_int32], C.c_int32),
         "cx_profile_read": ([h, P(C.c_int64), dp, dp], C.c_int32),
         "cx_launch_count": ([h, P(C.c_int64), C.c_int32], C.c_int32),
+        "cx_host_register": ([C.c_void_p, C.c_size_t], C.c_int32),
+        "cx_host_unregister": ([C.c_void_p], C.c_int32),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -98,6 +101,13 @@ class CxError(RuntimeError):
 
 
 def dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def cptr(a: np.ndarray):
+    """Pointer to a contiguous complex128 array as interleaved doubles."""
+    if a.dtype != np.complex128 or not (a.flags.c_contiguous or a.flags.f_contiguous):
+        raise ValueError("expected a contiguous complex128 array")
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 

@@ -600,6 +600,20 @@ cx_status cx_profile_read(cx_handle h, int64_t* launches, double* total_ms, doub
   return CX_OK;
 }
 
+cx_status cx_host_register(void* ptr, size_t bytes) {
+  if (!ptr || bytes == 0) return CX_ERR_ARG;
+  cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);
+  if (e != cudaSuccess) { g_create_err = std::string("cx_host_register: ") + cudaGetErrorString(e); return CX_ERR_CUDA; }
+  return CX_OK;
+}
+
+cx_status cx_host_unregister(void* ptr) {
+  if (!ptr) return CX_ERR_ARG;
+  cudaError_t e = cudaHostUnregister(ptr);
+  if (e != cudaSuccess) { g_create_err = std::string("cx_host_unregister: ") + cudaGetErrorString(e); return CX_ERR_CUDA; }
+  return CX_OK;
+}
+
 cx_status cx_launch_count(cx_handle h, int64_t* count, int32_t reset) {
   if (!h) return CX_ERR_ARG;
   if (count) *count = h->launches;

@@ -20,7 +20,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import CxError, check, dptr
+from ._lib import CxError, check, cptr, dptr
 
 __all__ = ["CyclixGPU", "attach", "h_nonlocal_vector_mult", "chebyshev_filter", "eigSolver", "poissonSolve", "CxError"]
 
@@ -92,11 +92,11 @@ class CyclixGPU:
     def set_psi(self, blk, psi):
         a = np.asfortranarray(psi, dtype=np.complex128)
         assert a.shape == (self.N, self.Ns[blk])
-        check(self.lib, self.h, self.lib.cx_set_psi(self.h, blk, dptr(a.view(np.float64))))
+        check(self.lib, self.h, self.lib.cx_set_psi(self.h, blk, cptr(a)))
 
     def get_psi(self, blk):
         a = np.empty((self.N, self.Ns[blk]), dtype=np.complex128, order="F")
-        check(self.lib, self.h, self.lib.cx_get_psi(self.h, blk, dptr(a.view(np.float64))))
+        check(self.lib, self.h, self.lib.cx_get_psi(self.h, blk, cptr(a)))
         return a
 
     # -- operators ---------------------------------------------------------------------------
@@ -105,15 +105,15 @@ class CyclixGPU:
         if X.ndim == 1:
             X = X[:, None]
         Y = np.empty_like(X, order="F")
-        check(self.lib, self.h, self.lib.cx_hpsi(self.h, blk, X.shape[1], dptr(X.view(np.float64)),
-                                                 dptr(Y.view(np.float64)), _lib.PREC[prec or self.prec]))
+        check(self.lib, self.h, self.lib.cx_hpsi(self.h, blk, X.shape[1], cptr(X),
+                                                 cptr(Y), _lib.PREC[prec or self.prec]))
         return Y
 
     def filter(self, blk, X, m, a, b, a0, prec=None):
         X = np.asfortranarray(X, dtype=np.complex128)
         Y = np.empty_like(X, order="F")
-        check(self.lib, self.h, self.lib.cx_chebyshev_filter(self.h, blk, X.shape[1], dptr(X.view(np.float64)),
-                                                             dptr(Y.view(np.float64)), int(m), float(a), float(b), float(a0),
+        check(self.lib, self.h, self.lib.cx_chebyshev_filter(self.h, blk, X.shape[1], cptr(X),
+                                                             cptr(Y), int(m), float(a), float(b), float(a0),
                                                              _lib.PREC[prec or self.prec]))
         return Y
 
@@ -125,9 +125,9 @@ class CyclixGPU:
                                                       dptr(bup), dptr(lambda_cutoff)))
 
     def eigsolve_host(self, count, npl, psi_packed, EigVal, a0, bup, lambda_cutoff, rhoTrigger=4):
-        assert psi_packed.dtype == np.complex128 and psi_packed.flags.c_contiguous or psi_packed.flags.f_contiguous
+        assert psi_packed.dtype == np.complex128 and (psi_packed.flags.c_contiguous or psi_packed.flags.f_contiguous)
         check(self.lib, self.h, self.lib.cx_eigsolver_host(self.h, int(count), int(npl), int(rhoTrigger),
-                                                           dptr(psi_packed.reshape(-1, order="A").view(np.float64)),
+                                                           cptr(psi_packed),
                                                            dptr(EigVal), dptr(a0), dptr(bup), dptr(lambda_cutoff)))
 
     def poisson(self, f, phi0=None, tol=1e-8, maxit=1000):

@@ -221,24 +221,42 @@ def _rot_pow(R: np.ndarray, p: int) -> np.ndarray:
 
 
 def _gaussian_field(S: CyclixS, centers: np.ndarray, amps: np.ndarray, width: float, cutoff: float) -> np.ndarray:
-    """sum_J amp_J exp(-|x - R_J|^2 / (2 width^2)) over all periodic images of R_J."""
+    """sum_J amp_J exp(-|x - R_J|^2 / (2 width^2)) over all periodic images of R_J (within ``cutoff``)."""
     r = S.xin + np.arange(S.Nx) * S.dx
     t = np.arange(S.Ny) * S.dy
     z = np.arange(S.Nz) * S.dz
     Rg, Tg, Zg = np.meshgrid(r, t, z, indexing="ij")
     nodes = noncart2cart(S, np.stack([Rg.reshape(-1, order="F"), Tg.reshape(-1, order="F"),
                                       Zg.reshape(-1, order="F")], axis=1))
+    zn = Zg.reshape(-1, order="F")
     out = np.zeros(S.N)
-    ny = int(math.ceil(2 * np.pi / S.L2)) // 2 + 1 if S.BCy == 0 else 0
+    # the distinct rotations of a cyclic group of order n_cyc = 2 pi / L2 (each counted once)
+    n_cyc = int(round(2 * np.pi / S.L2)) if S.BCy == 0 else 1
+    m_range = range(-(n_cyc // 2), n_cyc - n_cyc // 2)
     nz = int(math.ceil(cutoff / S.L3)) + 1 if S.BCz == 0 else 0
+    # angular extent of the cell (with the helical twist over its length) for a quick image cull
+    phi_lo = min(0.0, S.twist * S.L3)
+    phi_hi = S.L2 + max(0.0, S.twist * S.L3)
+    phi_c = 0.5 * (phi_lo + phi_hi)
     for J in range(centers.shape[0]):
-        for m in range(-ny, ny + 1):
+        for m in m_range:
             for n in range(-nz, nz + 1):
-                c = noncart2cart(S, np.array([[centers[J, 0], centers[J, 1] + m * S.L2,
-                                               centers[J, 2] + n * S.L3]]))[0]
-                d2 = ((nodes - c) ** 2).sum(axis=1)
-                msk = d2 < cutoff * cutoff
-                out[msk] += amps[J] * np.exp(-0.5 * d2[msk] / (width * width))
+                y, zz = centers[J, 1] + m * S.L2, centers[J, 2] + n * S.L3
+                if zz < -cutoff or zz > S.L3 + cutoff:
+                    continue
+                phi = y + S.twist * zz
+                phi = phi_c + math.remainder(phi - phi_c, 2 * math.pi)     # nearest copy of the angle
+                dphi = max(phi_lo - phi, phi - phi_hi, 0.0)
+                # every node has radius >= xin and angle >= dphi away from the image, hence distance
+                # >= 2 sqrt(r0 xin) sin(dphi / 2): cull images that cannot reach the cutoff
+                if 2 * math.sqrt(centers[J, 0] * S.xin) * math.sin(min(dphi, math.pi) / 2) > cutoff:
+                    continue
+                c = noncart2cart(S, np.array([[centers[J, 0], y, zz]]))[0]
+                msk = np.abs(zn - c[2]) < cutoff
+                d2 = ((nodes[msk] - c) ** 2).sum(axis=1)
+                inc = d2 < cutoff * cutoff
+                idx = np.nonzero(msk)[0][inc]
+                out[idx] += amps[J] * np.exp(-0.5 * d2[inc] / (width * width))
     return out
 
 

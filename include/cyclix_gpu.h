@@ -30,6 +30,7 @@
 #ifndef CYCLIX_GPU_H
 #define CYCLIX_GPU_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -153,6 +154,9 @@ cx_status cx_timer_stop(cx_handle h, double* ms);
  * launches and total ms since enabling). */
 cx_status cx_profile_stencil(cx_handle h, int32_t enable);
 cx_status cx_profile_read(cx_handle h, int64_t* launches, double* total_ms, double* bytes);
+/* Page-lock a caller-owned host buffer for faster copies (cudaHostRegister) and release it. */
+cx_status cx_host_register(void* ptr, size_t bytes);
+cx_status cx_host_unregister(void* ptr);
 /* Number of this library's kernel launches issued on h since the last reset. */
 cx_status cx_launch_count(cx_handle h, int64_t* count, int32_t reset);
 
