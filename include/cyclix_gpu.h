@@ -144,6 +144,18 @@ cx_status cx_eigsolver_host(cx_handle h, int32_t count, int32_t npl, int32_t rho
 cx_status cx_poisson(cx_handle h, const double* f, double* phi, double tol, int32_t maxit,
                      int32_t use_guess, int32_t* iters, double* relres);
 
+/* H*psi of block blk on caller-owned DEVICE buffers that allocates no device memory.
+ * No counterpart in the reference: it exists for callers that cannot let a library call
+ * cudaMalloc because another allocator owns their device memory (a framework's caching
+ * allocator, a MEX session that must leave nothing allocated when interrupted).
+ * X_dev, Y_dev: N x ncol column-major, complex128 (prec CX_PREC_FP64) or complex64
+ * (CX_PREC_MIXED), distinct.  The projector scratch lives in a fixed 16 MiB device array of
+ * the library (held by every GPU that loads it until exit); a call that needs more returns
+ * CX_ERR_ARG naming the largest ncol that fits.  The first call on a device looks up that
+ * array's address and should come before any stream capture.  Calls share the array: calls
+ * whose work overlaps on the GPU race.  Each call waits for its own work before returning. */
+cx_status cx_hpsi_noalloc(cx_handle h, int32_t blk, int32_t ncol, const void* X_dev, void* Y_dev, int32_t prec);
+
 /* ---- measurement -------------------------------------------------------- */
 /* Wait for all work of h. */
 cx_status cx_sync(cx_handle h);
