@@ -222,6 +222,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--only-mixed", action="store_true",
+                    help="profiling mode: time only the mixed-precision device-resident steps (no CPU baseline, FP64 arm or e2e)")
+    ap.add_argument("--workload", default=WORKLOAD, help="workload name (profiling mode)")
     args = ap.parse_args()
     warmup = max(3, args.warmup)
     rank = env_int("RANK", 0)
@@ -252,6 +255,19 @@ def main():
                 "e2e": {"value": round(v, 3), "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
                 "note": "the reference is MATLAB (not installable here); this arm times the NumPy/SciPy restatement of it"}
         print(json.dumps(line), flush=True)
+        return 0
+
+    if args.only_mixed:
+        wlp = WORKLOADS[args.workload]
+        S = make_system(wlp)
+        g, ms, launches, _, prof, _, _ = gpu_step_times(S, block_layout(wlp, S), "mixed", args.steps, warmup, wlp.npl,
+                                                        profile_stencil=True)
+        g.close()
+        n_launch, stencil_ms, stencil_bytes = prof
+        print(json.dumps({"mode": "only-mixed", "workload": args.workload, "ms_per_step": round(ms, 3),
+                          "stencil_avg_ms": round(stencil_ms / max(n_launch, 1), 4),
+                          "stencil_gbs": round(stencil_bytes / (stencil_ms * 1e-3) / 1e9, 1) if stencil_ms > 0 else None,
+                          "launches_per_step": launches}), flush=True)
         return 0
 
     dist = None

@@ -6,6 +6,8 @@
 #include <algorithm>
 #include <complex>
 
+#include <cuda.h>
+
 #include "cx_internal.h"
 #include "cx_common.h"
 
@@ -45,6 +47,7 @@ void free_blocks(cx_handle h) {
   cudaFree(h->d_state_tab); h->d_state_tab = nullptr;
   cudaFree(h->d_cprime); h->d_cprime = nullptr;
   cudaFree(h->d_seg_phase); h->d_seg_phase = nullptr;
+  cudaFree(h->d_maps); h->d_maps = nullptr;
   h->nl.seg_phase = nullptr;
   h->nblk = 0;
   h->nstates = 0;
@@ -74,6 +77,7 @@ cx_status make_block_devs(cx_handle h, const std::vector<cplx<R>*>& b0, const st
     d.ph_zr = k3 == 0 ? make_double2(1, 0) : cexp_i(k3 * h->grid.L3);
     d.Ns = B.Ns;
     d.state0 = st;
+    d.veff_spin = B.spin;
     st += B.Ns;
     out.push_back(d);
   }
@@ -111,7 +115,7 @@ void cheb_scalars(int m, double a, double b, double a0, std::vector<StepScalars>
 // Launch one fused step over the given block set and account profiling.
 template <typename R>
 cx_status fused_step(cx_handle h, const BlockDev<R>* d_blocks, const StepScalars* d_scal, int nblk, const int2* d_state_tab,
-                     int nstates, int in_sel, bool use_xprev, cplx<R>* cprime, bool nonlocal, double bytes) {
+                     int nstates, int in_sel, bool use_xprev, cplx<R>* cprime, bool nonlocal, double bytes, const void* maps) {
   const NonlocalDev* nlp = nullptr;
   NonlocalDev nl = h->nl;
   if (nonlocal && nl.nseg > 0) {
@@ -121,16 +125,33 @@ cx_status fused_step(cx_handle h, const BlockDev<R>* d_blocks, const StepScalars
     h->launches++;
     nlp = &nl;
   }
+  const bool tma = (sizeof(R) == 4) && maps && h->use_tma;
   if (h->prof) CX_TRY_CUDA(h, cudaEventRecord(h->ev0, h->stream));
-  CX_TRY_CUDA(h, launch_cheb_step<R>(h->g, h->coef, d_blocks, d_scal, nblk, d_state_tab, nstates, in_sel, use_xprev, nlp,
-                                     cprime, h->stream));
+  if constexpr (sizeof(R) == 4) {
+    if (tma) {
+      // stencil without the projector term, then the projector apply on the touched row chunks
+      CX_TRY_CUDA(h, launch_cheb_step_tma(h->g, h->coef, (const BlockDev<float>*)d_blocks, d_scal, d_state_tab, nstates, in_sel,
+                                          use_xprev, *(const TmaMapSet*)maps, h->d_status, h->stream));
+    }
+  }
+  if (!tma)
+    CX_TRY_CUDA(h, launch_cheb_step<R>(h->g, h->coef, d_blocks, d_scal, nblk, d_state_tab, nstates, in_sel, use_xprev, nlp, cprime,
+                                       h->stream));
   h->launches++;
+  if (h->prof) CX_TRY_CUDA(h, cudaEventRecord(h->ev1, h->stream));
+  if (tma && nlp) {
+    CX_TRY_CUDA(h, launch_nl_apply<R>(h->g, d_blocks, d_scal, d_state_tab, nstates, in_sel ^ 1, h->d_chunks, h->nchunks,
+                                      h->d_ent_start, h->d_ent_count, *nlp, cprime, h->stream));
+    h->launches++;
+  }
   if (h->prof) {
-    CX_TRY_CUDA(h, cudaEventRecord(h->ev1, h->stream));
-    CX_TRY_CUDA(h, cudaEventSynchronize(h->ev1));
-    float ms = 0;
+    CX_TRY_CUDA(h, cudaEventRecord(h->tev1, h->stream));
+    CX_TRY_CUDA(h, cudaEventSynchronize(h->tev1));
+    float ms = 0, ms2 = 0;
     CX_TRY_CUDA(h, cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+    CX_TRY_CUDA(h, cudaEventElapsedTime(&ms2, h->ev1, h->tev1));
     h->prof_ms += ms;
+    h->prof_apply_ms += ms2;
     h->prof_launches++;
     h->prof_bytes += bytes;
   }
@@ -141,7 +162,7 @@ cx_status fused_step(cx_handle h, const BlockDev<R>* d_blocks, const StepScalars
 template <typename R>
 cx_status filter_blocks(cx_handle h, const BlockDev<R>* d_blocks, int nblk, const int2* d_state_tab, int nstates,
                         size_t total_elems, int sel0, int m, const std::vector<double>& a, const std::vector<double>& b,
-                        const std::vector<double>& a0, cplx<R>* cprime, int* sel_out) {
+                        const std::vector<double>& a0, cplx<R>* cprime, int* sel_out, const void* maps) {
   if (m < 1) { h->err = "filter degree must be >= 1"; return CX_ERR_ARG; }
   std::vector<StepScalars> sc((size_t)m * nblk);
   for (int i = 0; i < nblk; ++i) cheb_scalars(m, a[i], b[i], a0[i], sc, nblk, i);
@@ -158,7 +179,7 @@ cx_status filter_blocks(cx_handle h, const BlockDev<R>* d_blocks, int nblk, cons
   for (int d = 1; d <= m; ++d) {
     const int in_sel = sel0 ^ ((d - 1) & 1);
     cx_status s = fused_step<R>(h, d_blocks, h->d_scal + (size_t)(d - 1) * nblk, nblk, d_state_tab, nstates, in_sel, d >= 2,
-                                cprime, true, (d >= 2 ? 3.0 : 2.0) * sz);
+                                cprime, true, (d >= 2 ? 3.0 : 2.0) * sz, maps);
     if (s != CX_OK) return s;
   }
   *sel_out = sel0 ^ (m & 1);
@@ -167,18 +188,53 @@ cx_status filter_blocks(cx_handle h, const BlockDev<R>* d_blocks, int nblk, cons
 
 template cx_status filter_blocks<float>(cx_handle, const BlockDev<float>*, int, const int2*, int, size_t, int, int,
                                         const std::vector<double>&, const std::vector<double>&, const std::vector<double>&,
-                                        cplx<float>*, int*);
+                                        cplx<float>*, int*, const void*);
 template cx_status filter_blocks<double>(cx_handle, const BlockDev<double>*, int, const int2*, int, size_t, int, int,
                                          const std::vector<double>&, const std::vector<double>&, const std::vector<double>&,
-                                         cplx<double>*, int*);
+                                         cplx<double>*, int*, const void*);
 template cx_status make_block_devs<float>(cx_handle, const std::vector<cplx<float>*>&, const std::vector<cplx<float>*>&,
                                           const std::vector<int>&, std::vector<BlockDev<float>>&);
 template cx_status make_block_devs<double>(cx_handle, const std::vector<cplx<double>*>&, const std::vector<cplx<double>*>&,
                                            const std::vector<int>&, std::vector<BlockDev<double>>&);
 template cx_status fused_step<float>(cx_handle, const BlockDev<float>*, const StepScalars*, int, const int2*, int, int, bool,
-                                     cplx<float>*, bool, double);
+                                     cplx<float>*, bool, double, const void*);
 template cx_status fused_step<double>(cx_handle, const BlockDev<double>*, const StepScalars*, int, const int2*, int, int, bool,
-                                      cplx<double>*, bool, double);
+                                      cplx<double>*, bool, double, const void*);
+
+cx_status build_maps(cx_handle h, const std::vector<const void*>& p0, const std::vector<const void*>& p1, const std::vector<int>& Ns,
+                     void** d_maps, TmaMapSet* set) {
+  *d_maps = nullptr;
+  const size_t nb = p0.size();
+  std::vector<CUtensorMap_st> maps(4 * nb);
+  for (size_t b = 0; b < nb; ++b) {
+    cx_status s = make_buffer_maps(h, p0[b], Ns[b], &maps[2 * b], &maps[2 * nb + 2 * b]);
+    if (s != CX_OK) return s;
+    if ((s = make_buffer_maps(h, p1[b], Ns[b], &maps[2 * b + 1], &maps[2 * nb + 2 * b + 1])) != CX_OK) return s;
+  }
+  void* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, maps.size() * sizeof(CUtensorMap_st));
+  if (e != cudaSuccess) { h->err = std::string("tensor maps: ") + cudaGetErrorString(e); return CX_ERR_NOMEM; }
+  e = cudaMemcpy(d, maps.data(), maps.size() * sizeof(CUtensorMap_st), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) { cudaFree(d); h->err = std::string("tensor maps: ") + cudaGetErrorString(e); return CX_ERR_CUDA; }
+  *d_maps = d;
+  set->xmaps = d;
+  set->omaps = (const CUtensorMap_st*)d + 2 * nb;
+  set->vmaps = h->d_fmaps;
+  return CX_OK;
+}
+
+cx_status check_pipeline_status(cx_handle h) {
+  if (!h->d_status) return CX_OK;
+  int st = 0;
+  CX_TRY_CUDA(h, cudaMemcpyAsync(&st, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CX_TRY_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (st != 0) {
+    CX_TRY_CUDA(h, cudaMemset(h->d_status, 0, sizeof(int)));
+    h->err = "stencil pipeline: a bulk-copy wait exceeded its iteration limit (results of this call are invalid)";
+    return CX_ERR_CUDA;
+  }
+  return CX_OK;
+}
 
 // A one-block scratch view (used by the host-buffer entry points): temporary buffers of ncol columns.
 template <typename R>
@@ -190,9 +246,11 @@ struct ScratchView {
   int2* d_tab = nullptr;
   StepScalars* d_scal = nullptr;
   double2* d_ph = nullptr;
-  double2* saved_ph = nullptr;
+  void* d_maps = nullptr;
+  TmaMapSet set{};
   ~ScratchView() {
     cudaFree(b0); cudaFree(b1); cudaFree(cprime); cudaFree(d_blk); cudaFree(d_tab); cudaFree(d_scal); cudaFree(d_ph);
+    cudaFree(d_maps);
   }
 };
 
@@ -217,6 +275,9 @@ cx_status make_scratch(cx_handle h, int blk, int ncol, ScratchView<R>& v) {
   CX_TRY_CUDA(h, cudaMemcpy(v.d_tab, tab.data(), sizeof(int2) * ncol, cudaMemcpyHostToDevice));
   std::vector<double2> ph = segment_phases(h, h->blocks[blk]);
   if (!ph.empty()) CX_TRY_CUDA(h, cudaMemcpy(v.d_ph, ph.data(), sizeof(double2) * ph.size(), cudaMemcpyHostToDevice));
+  if (sizeof(R) == 4 && h->tma_ok) {
+    if ((s = build_maps(h, {v.b0}, {v.b1}, {ncol}, &v.d_maps, &v.set)) != CX_OK) return s;
+  }
   return CX_OK;
 }
 
@@ -232,9 +293,10 @@ static cx_status hpsi_T(cx_handle h, int blk, int ncol, const double* X, double*
   CX_TRY_CUDA(h, cudaMemcpy(v.d_scal, &one, sizeof(one), cudaMemcpyHostToDevice));
   const double2* saved = h->nl.seg_phase;
   h->nl.seg_phase = v.d_ph;
-  s = fused_step<R>(h, v.d_blk, v.d_scal, 1, v.d_tab, ncol, 0, false, v.cprime, true, 2.0 * n * sizeof(cplx<R>));
+  s = fused_step<R>(h, v.d_blk, v.d_scal, 1, v.d_tab, ncol, 0, false, v.cprime, true, 2.0 * n * sizeof(cplx<R>), v.d_maps ? &v.set : nullptr);
   h->nl.seg_phase = saved;
   if (s != CX_OK) return s;
+  if ((s = check_pipeline_status(h)) != CX_OK) return s;
   return cx_dev_to_host(h, v.b1, Y, n, sizeof(R) == 8 ? CX_PREC_FP64 : CX_PREC_MIXED);
 }
 
@@ -254,7 +316,8 @@ static cx_status filter_T(cx_handle h, int blk, int ncol, const double* X, doubl
   h->scal_cap = 0;
   int sel = 0;
   s = filter_blocks<R>(h, v.d_blk, 1, v.d_tab, ncol, n, 0, m, std::vector<double>{a}, std::vector<double>{b},
-                       std::vector<double>{a0}, v.cprime, &sel);
+                       std::vector<double>{a0}, v.cprime, &sel, v.d_maps ? &v.set : nullptr);
+  if (s == CX_OK) s = check_pipeline_status(h);
   v.d_scal = h->d_scal;            // freed with the view
   h->d_scal = saved_scal;
   h->scal_cap = saved_cap;
@@ -329,6 +392,8 @@ cx_status cx_create(const cx_grid* grid, int32_t n_atm, const cx_atom* atoms, in
   cx_status s;
   if ((s = upload(h, &h->d_W, h->W)) != CX_OK) { g_create_err = h->err; cx_destroy(h); return s; }
   if ((s = dalloc(h, &h->d_veff, (size_t)N * nspin)) != CX_OK) { g_create_err = h->err; cx_destroy(h); return s; }
+  if ((s = dalloc(h, &h->d_status, 1)) != CX_OK) { g_create_err = h->err; cx_destroy(h); return s; }
+  CX_TRY_CUDA(h, cudaMemset(h->d_status, 0, sizeof(int)));
   CX_TRY_CUDA(h, cudaMemset(h->d_veff, 0, sizeof(double) * (size_t)N * nspin));
 
   // ---- nonlocal tables
@@ -411,6 +476,35 @@ cx_status cx_create(const cx_grid* grid, int32_t n_atm, const cx_atom* atoms, in
   h->nl.atom_node_ptr = d_anp; h->nl.node_pos = d_np; h->nl.node_seg = d_ns; h->nl.atom_seg_ptr = d_asp;
   h->nl.angnum = d_an; h->nl.row_ptr = d_rp; h->nl.ent_seg = d_es; h->nl.gamma = d_g;
   h->d_node_wchi64 = d_w64; h->d_ent_chi64 = d_c64; h->d_node_wchi32 = d_w32; h->d_ent_chi32 = d_c32;
+  // TMA path: per-point entry start / count, float Veff and the field maps
+  h->tma_ok = tma_eligible(h->g, sizeof(float2));
+  if (h->tma_ok) {
+    std::vector<int32_t> est(row_ptr.begin(), row_ptr.end() - 1), ecnt(N);
+    for (int p = 0; p < N; ++p) ecnt[p] = row_ptr[p + 1] - row_ptr[p];
+    std::vector<int> chunks;
+    for (int row = 0; row < N / G.Nx; ++row)
+      for (int r0 = 0; r0 < G.Nx; r0 += 32) {
+        const int p0 = row * G.Nx + r0;
+        if (row_ptr[std::min(p0 + 32, (row + 1) * G.Nx)] > row_ptr[p0]) chunks.push_back(p0);
+      }
+    h->nchunks = (int)chunks.size();
+    if ((s = upload(h, &h->d_chunks, chunks)) || (s = upload(h, &h->d_ent_start, est)) || (s = upload(h, &h->d_ent_count, ecnt)) ||
+        (s = dalloc(h, &h->d_veff32, (size_t)N * nspin))) {
+      g_create_err = h->err;
+      cx_destroy(h);
+      return s;
+    }
+    CX_TRY_CUDA(h, cudaMemset(h->d_veff32, 0, sizeof(float) * (size_t)N * nspin));
+    std::vector<CUtensorMap_st> fm(nspin);
+    for (int sp = 0; sp < nspin; ++sp)
+      if ((s = make_field_map(h, h->d_veff32 + (size_t)sp * N, false, &fm[sp])) != CX_OK) { g_create_err = h->err; cx_destroy(h); return s; }
+    if (cudaMalloc(&h->d_fmaps, fm.size() * sizeof(CUtensorMap_st)) != cudaSuccess ||
+        cudaMemcpy(h->d_fmaps, fm.data(), fm.size() * sizeof(CUtensorMap_st), cudaMemcpyHostToDevice) != cudaSuccess) {
+      g_create_err = "cx_create: field tensor maps";
+      cx_destroy(h);
+      return CX_ERR_NOMEM;
+    }
+  }
   *out = h;
   return CX_OK;
 }
@@ -421,6 +515,9 @@ cx_status cx_destroy(cx_handle h) {
   free_blocks(h);
   for (void* p : h->nl_allocs) cudaFree(p);
   cudaFree(h->d_veff);
+  cudaFree(h->d_veff32);
+  cudaFree(h->d_fmaps);
+  cudaFree(h->d_status);
   cudaFree(h->d_scal);
   cudaFree(h->d_ws);
   cudaFreeHost(h->h_ws);
@@ -437,9 +534,19 @@ cx_status cx_destroy(cx_handle h) {
   return CX_OK;
 }
 
+__global__ void k_veff32(const double* __restrict__ a, float* __restrict__ b, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) b[i] = (float)a[i];
+}
+
 cx_status cx_set_veff(cx_handle h, const double* Veff) {
   if (!h || !Veff) return CX_ERR_ARG;
   CX_TRY_CUDA(h, cudaMemcpyAsync(h->d_veff, Veff, sizeof(double) * (size_t)h->g.N * h->nspin, cudaMemcpyHostToDevice, h->stream));
+  if (h->d_veff32) {
+    const size_t n = (size_t)h->g.N * h->nspin;
+    k_veff32<<<(unsigned)std::min<size_t>((n + 255) / 256, 152 * 16), 256, 0, h->stream>>>(h->d_veff, h->d_veff32, n);
+    h->launches++;
+    CX_TRY_CUDA(h, cudaGetLastError());
+  }
   CX_TRY_CUDA(h, cudaStreamSynchronize(h->stream));
   return CX_OK;
 }
@@ -519,6 +626,12 @@ cx_status cx_set_blocks(cx_handle h, int32_t nblk, const cx_block* blocks, int32
     if ((s = dalloc(h, &d, bd.size())) != CX_OK) { free_blocks(h); return s; }
     CX_TRY_CUDA(h, cudaMemcpy(d, bd.data(), sizeof(bd[0]) * bd.size(), cudaMemcpyHostToDevice));
     h->d_blocks = d;
+    if (h->tma_ok) {
+      std::vector<const void*> q0(p0.begin(), p0.end()), q1(p1.begin(), p1.end());
+      std::vector<int> ns;
+      for (int b = 0; b < nblk; ++b) ns.push_back(blocks[b].Ns);
+      if ((s = build_maps(h, q0, q1, ns, &h->d_maps, &h->tma_main)) != CX_OK) { free_blocks(h); return s; }
+    }
   }
   return CX_OK;
 }
@@ -588,7 +701,14 @@ cx_status cx_profile_stencil(cx_handle h, int32_t enable) {
   h->prof = enable != 0;
   h->prof_launches = 0;
   h->prof_ms = 0;
+  h->prof_apply_ms = 0;
   h->prof_bytes = 0;
+  return CX_OK;
+}
+
+cx_status cx_profile_read_apply(cx_handle h, double* apply_ms) {
+  if (!h || !apply_ms) return CX_ERR_ARG;
+  *apply_ms = h->prof_apply_ms;
   return CX_OK;
 }
 

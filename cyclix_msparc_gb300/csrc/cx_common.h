@@ -20,10 +20,20 @@ void cheb_scalars(int m, double a, double b, double a0, std::vector<StepScalars>
 
 template <typename R>
 cx_status fused_step(cx_handle h, const BlockDev<R>* d_blocks, const StepScalars* d_scal, int nblk, const int2* d_state_tab,
-                     int nstates, int in_sel, bool use_xprev, cplx<R>* cprime, bool nonlocal, double bytes);
+                     int nstates, int in_sel, bool use_xprev, cplx<R>* cprime, bool nonlocal, double bytes,
+                     const void* maps = nullptr);
 template <typename R>
 cx_status filter_blocks(cx_handle h, const BlockDev<R>* d_blocks, int nblk, const int2* d_state_tab, int nstates,
                         size_t total_elems, int sel0, int m, const std::vector<double>& a, const std::vector<double>& b,
-                        const std::vector<double>& a0, cplx<R>* cprime, int* sel_out);
+                        const std::vector<double>& a0, cplx<R>* cprime, int* sel_out, const void* maps = nullptr);
+// tensor maps of one complex64 buffer of Ns states / of a 4-byte grid field (cx_stencil_tma.cu)
+cx_status make_buffer_maps(cx_handle h, const void* base, int Ns, struct CUtensorMap_st* xmap, struct CUtensorMap_st* omap);
+cx_status make_field_map(cx_handle h, const void* base, bool is_int, struct CUtensorMap_st* out);
+// build the X / output maps of device buffers p0/p1 of a block set into a new device array and
+// fill the block part of *set (the field maps of the handle complete it)
+cx_status build_maps(cx_handle h, const std::vector<const void*>& p0, const std::vector<const void*>& p1,
+                     const std::vector<int>& Ns, void** d_maps, TmaMapSet* set);
+// status flag of the TMA pipeline: CX_OK, or CX_ERR_CUDA with a message when a CTA timed out
+cx_status check_pipeline_status(cx_handle h);
 
 }  // namespace cx

@@ -54,7 +54,8 @@ template <typename R> struct BlockDev {
   double2 ph_zl, ph_zr;      // z wrap phases exp(-+ i k3 L3)
   int32_t Ns;
   int32_t state0;            // first global state index of this block
-  int32_t pad[2];
+  int32_t veff_spin;         // spin channel (selects the Veff map of the TMA path)
+  int32_t pad;
 };
 
 // Chebyshev step scalars of one block for one degree: out = alpha*(H*in - c*in) + beta*xprev
@@ -90,8 +91,24 @@ cudaError_t launch_cheb_step(const GridDev& g, const StencilCoef& coef, const Bl
                              int in_sel, bool use_xprev, const NonlocalDev* nl, const cplx<R>* cprime,
                              cudaStream_t st);
 template <typename R>
+cudaError_t launch_nl_apply(const GridDev& g, const BlockDev<R>* blocks, const StepScalars* scal, const int2* state_tab, int nstates,
+                            int out_sel, const int* chunks, int nchunks, const int32_t* ent_start, const int32_t* ent_count,
+                            const NonlocalDev& nl, const cplx<R>* cprime, cudaStream_t st);
+template <typename R>
 cudaError_t launch_nl_contract(const GridDev& g, const BlockDev<R>* blocks, const int2* state_tab, int nstates,
                                int in_sel, const NonlocalDev& nl, cplx<R>* cprime, cudaStream_t st);
+
+// ---------------------------------------------------------------- TMA path (cx_stencil_tma.cu)
+// Device arrays of tensor maps used by one launch of the TMA kernel.
+struct TmaMapSet {
+  const void* xmaps;         // [block][buffer] complex64 X maps (staged tile box)
+  const void* omaps;         // [block][buffer] complex64 output-tile maps
+  const void* vmaps;         // [spin] float Veff maps
+};
+bool tma_eligible(const GridDev& g, int elem_bytes);
+cudaError_t launch_cheb_step_tma(const GridDev& g, const StencilCoef& coef, const BlockDev<float>* blocks, const StepScalars* scal,
+                                 const int2* state_tab, int nstates, int in_sel, bool use_xprev, const TmaMapSet& maps, int* status,
+                                 cudaStream_t st);
 
 }  // namespace cx
 
@@ -150,11 +167,24 @@ struct cx_handle_s {
   void* d_misc = nullptr; size_t misc_bytes = 0;     // column norms, permutations, status
   void* d_pois = nullptr; size_t pois_bytes = 0;     // Poisson (AAR) vectors
 
+  // TMA path (complex64): float Veff, per-point projector entry start / count, tensor maps
+  float* d_veff32 = nullptr;
+  int32_t* d_ent_start = nullptr;
+  int32_t* d_ent_count = nullptr;
+  int* d_chunks = nullptr;                           // 32-point row chunks touched by a projector ball
+  int nchunks = 0;
+  void* d_fmaps = nullptr;                           // [nspin] Veff maps
+  void* d_maps = nullptr;                            // block buffers: [nblk][2] X maps, then [nblk][2] output maps
+  cx::TmaMapSet tma_main{};
+  bool tma_ok = false;                               // operator eligible for the TMA kernel
+  int* d_status = nullptr;
+  bool use_tma = true;
+
   // profiling
   bool prof = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, tev0 = nullptr, tev1 = nullptr;
   int64_t prof_launches = 0;
-  double prof_ms = 0, prof_bytes = 0;
+  double prof_ms = 0, prof_bytes = 0, prof_apply_ms = 0;
   int64_t launches = 0;
 };
 

@@ -494,15 +494,16 @@ static cx_status eigsolver_T(cx_handle h, int count, int npl, int rhoTrigger, do
   for (int b = 0; b < nblk; ++b) tot += (size_t)h->g.N * h->blocks[b].Ns;
   int sel = 0;
   cx_status s = filter_blocks<R>(h, (const BlockDev<R>*)h->d_blocks, nblk, h->d_state_tab, h->nstates, tot, h->psi_sel[0], npl, va,
-                                 vb, va0, (cplx<R>*)h->d_cprime, &sel);
+                                 vb, va0, (cplx<R>*)h->d_cprime, &sel, h->d_maps ? &h->tma_main : nullptr);
   if (s != CX_OK) return s;
   // ---- H * X for all blocks (into the other buffer)
   {
     std::vector<StepScalars> one(nblk, StepScalars{1.0, 0.0, 0.0, 0.0});
     CX_TRY_CUDA(h, cudaMemcpyAsync(h->d_scal, one.data(), nblk * sizeof(StepScalars), cudaMemcpyHostToDevice, h->stream));
     s = fused_step<R>(h, (const BlockDev<R>*)h->d_blocks, h->d_scal, nblk, h->d_state_tab, h->nstates, sel, false,
-                      (cplx<R>*)h->d_cprime, true, 2.0 * tot * sizeof(cplx<R>));
+                      (cplx<R>*)h->d_cprime, true, 2.0 * tot * sizeof(cplx<R>), h->d_maps ? &h->tma_main : nullptr);
     if (s != CX_OK) return s;
+    if ((s = check_pipeline_status(h)) != CX_OK) return s;
   }
   // ---- Rayleigh-Ritz per block
   int nmax = 0;

@@ -268,6 +268,61 @@ nl_contract_kernel(const int N, const BlockDev<R>* __restrict__ blocks, const in
   }
 }
 
+// Kleinman-Bylander apply as its own pass (used after the TMA stencil, which leaves it out):
+//   out[p, s] += alpha_b * sum_{entries e of p} Chi_e . Cp[s][seg_e][:]
+// (the scatter of src/h_nonlocal_vector_mult.m:38-42, scaled like the rest of the Chebyshev step).
+// A CTA owns one 32-point row chunk (a radial tile row that some projector ball touches) and 8 states
+// (one per warp): the chunk's entries are read once from L2 and reused by the 8 warps from L1.
+template <typename R>
+__global__ void __launch_bounds__(256)
+nl_apply_kernel(const int N, const int Nx, const BlockDev<R>* __restrict__ blocks, const StepScalars* __restrict__ scal,
+                const int2* __restrict__ state_tab, const int nstates, const int out_sel, const int* __restrict__ chunks,
+                const int32_t* __restrict__ ent_start, const int32_t* __restrict__ ent_count, const int32_t* __restrict__ ent_seg,
+                const R* __restrict__ ent_chi, const cplx<R>* __restrict__ cprime, const int nseg) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int gs = blockIdx.y * 8 + w;
+  if (gs >= nstates) return;
+  const int p0 = chunks[blockIdx.x];
+  const int r = p0 % Nx + lane;
+  if (r >= Nx) return;
+  const int p = p0 + lane;
+  const int e0 = ent_start[p], ne = ent_count[p];
+  if (ne == 0) return;
+  const int2 bs = state_tab[gs];
+  const cplx<R>* cp = cprime + (size_t)gs * nseg * kAngMax;
+  cplx<R> acc = mk<R>((R)0, (R)0);
+  for (int e = e0; e < e0 + ne; ++e) {
+    const cplx<R>* cs = cp + (size_t)ent_seg[e] * kAngMax;
+    const R* ch = ent_chi + (size_t)e * kAngMax;
+#pragma unroll
+    for (int q = 0; q < kAngMax; ++q) cfma(acc, ch[q], cs[q]);
+  }
+  const R alpha = (R)scal[bs.x].alpha;
+  cplx<R>* out = blocks[bs.x].buf[out_sel] + (size_t)bs.y * N + p;
+  cplx<R> o = *out;
+  o.x = fma(alpha, acc.x, o.x);
+  o.y = fma(alpha, acc.y, o.y);
+  *out = o;
+}
+
+template <typename R>
+cudaError_t launch_nl_apply(const GridDev& g, const BlockDev<R>* blocks, const StepScalars* scal, const int2* state_tab, int nstates,
+                            int out_sel, const int* chunks, int nchunks, const int32_t* ent_start, const int32_t* ent_count,
+                            const NonlocalDev& nl, const cplx<R>* cprime, cudaStream_t st) {
+  if (nchunks == 0 || nl.nseg == 0) return cudaSuccess;
+  dim3 grid((unsigned)nchunks, (unsigned)((nstates + 7) / 8));
+  if (grid.y > 65535) return cudaErrorInvalidConfiguration;
+  nl_apply_kernel<R><<<grid, 256, 0, st>>>(g.N, g.Nx, blocks, scal, state_tab, nstates, out_sel, chunks, ent_start, ent_count, nl.ent_seg,
+                                           (const R*)nl.ent_chi, cprime, nl.nseg);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_nl_apply<float>(const GridDev&, const BlockDev<float>*, const StepScalars*, const int2*, int, int, const int*,
+                                            int, const int32_t*, const int32_t*, const NonlocalDev&, const cplx<float>*, cudaStream_t);
+template cudaError_t launch_nl_apply<double>(const GridDev&, const BlockDev<double>*, const StepScalars*, const int2*, int, int,
+                                             const int*, int, const int32_t*, const int32_t*, const NonlocalDev&, const cplx<double>*,
+                                             cudaStream_t);
+
 template <typename R, int F, bool HEL>
 static cudaError_t launch_one(const StepArgs<R>& a, dim3 grid, cudaStream_t st) {
   cheb_step_kernel<R, F, HEL><<<grid, NTHR, 0, st>>>(a);

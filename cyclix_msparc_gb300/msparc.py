@@ -163,6 +163,11 @@ class CyclixGPU:
         check(self.lib, self.h, self.lib.cx_profile_read(self.h, C.byref(n), C.byref(ms), C.byref(by)))
         return n.value, ms.value, by.value
 
+    def profile_read_apply(self) -> float:
+        ms = C.c_double(0)
+        check(self.lib, self.h, self.lib.cx_profile_read_apply(self.h, C.byref(ms)))
+        return ms.value
+
     def launch_count(self, reset=False) -> int:
         n = C.c_int64(0)
         check(self.lib, self.h, self.lib.cx_launch_count(self.h, C.byref(n), 1 if reset else 0))

@@ -166,6 +166,9 @@ cx_status cx_timer_stop(cx_handle h, double* ms);
  * launches and total ms since enabling). */
 cx_status cx_profile_stencil(cx_handle h, int32_t enable);
 cx_status cx_profile_read(cx_handle h, int64_t* launches, double* total_ms, double* bytes);
+/* Device time (ms) of the separate projector-apply launches that follow the complex64 stencil
+ * launches, over the same profiling window (0 for the complex128 path, which fuses it). */
+cx_status cx_profile_read_apply(cx_handle h, double* apply_ms);
 /* Page-lock a caller-owned host buffer for faster copies (cudaHostRegister) and release it. */
 cx_status cx_host_register(void* ptr, size_t bytes);
 cx_status cx_host_unregister(void* ptr);
