@@ -20,7 +20,7 @@ PREC = {"fp64": CX_PREC_FP64, "mixed": CX_PREC_MIXED}
 EXPORTS = ["cx_create", "cx_destroy", "cx_last_error", "cx_version", "cx_set_blocks", "cx_set_veff", "cx_set_psi",
            "cx_get_psi", "cx_hpsi", "cx_chebyshev_filter", "cx_eigsolver", "cx_eigsolver_host", "cx_poisson", "cx_sync",
            "cx_timer_start", "cx_timer_stop", "cx_profile_stencil", "cx_profile_read", "cx_launch_count",
-           "cx_host_register", "cx_host_unregister", "cx_hpsi_noalloc", "cx_profile_read_apply"]
+           "cx_host_register", "cx_host_unregister", "cx_hpsi_noalloc", "cx_profile_read_apply", "cx_eig_fallback_count"]
 
 
 class cx_grid(C.Structure):
@@ -87,6 +87,7 @@ def load(build_if_missing: bool = True):
         "cx_host_unregister": ([C.c_void_p], C.c_int32),
         "cx_hpsi_noalloc": ([h, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32], C.c_int32),
         "cx_profile_read_apply": ([h, dp], C.c_int32),
+        "cx_eig_fallback_count": ([h, P(C.c_int64)], C.c_int32),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

@@ -186,6 +186,7 @@ struct cx_handle_s {
   int64_t prof_launches = 0;
   double prof_ms = 0, prof_bytes = 0, prof_apply_ms = 0;
   int64_t launches = 0;
+  int64_t eig_fallbacks = 0;                         // subspace eigensolves that needed the general solver
 };
 
 #define CX_TRY_CUDA(h, expr)                                                                 \

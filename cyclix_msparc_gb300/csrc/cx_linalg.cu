@@ -82,6 +82,74 @@ __global__ void k_gather_cols(const double2* __restrict__ in, double2* __restric
   }
 }
 
+// ------------------------------------------------------------------ subspace eigensolver kernels
+// WX = W .* X (column-major N x n)
+template <typename R>
+__global__ void k_wscale(const cplx<R>* __restrict__ X, cplx<R>* __restrict__ Y, const double* __restrict__ W, int N, int n) {
+  const size_t tot = (size_t)N * n;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
+    const R w = (R)W[i % N];
+    Y[i].x = X[i].x * w;
+    Y[i].y = X[i].y * w;
+  }
+}
+// Th = (T + T^H) / 2
+__global__ void k_herm_part(const double2* __restrict__ T, double2* __restrict__ Th, int n) {
+  const size_t tot = (size_t)n * n;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = i % n, c = i / n;
+    const double2 a = T[i], b = T[r * n + c];
+    Th[i] = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y));
+  }
+}
+// split B into its diagonal d and the off-diagonal part E (in place); Z = 0
+__global__ void k_split_diag(double2* __restrict__ B, double2* __restrict__ d, double2* __restrict__ Z, int n) {
+  const size_t tot = (size_t)n * n;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = i % n, c = i / n;
+    if (r == c) { d[r] = B[i]; B[i] = make_double2(0, 0); }
+    Z[i] = make_double2(0, 0);
+  }
+}
+__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
+  const double den = b.x * b.x + b.y * b.y;
+  return make_double2((a.x * b.x + a.y * b.y) / den, (a.y * b.x - a.x * b.y) / den);
+}
+// one fixed-point sweep of B X = X Lambda with X = I + Z (Z zero on the diagonal), B = diag(d) + E:
+//   lambda_j = d_j + (E Z)_jj ,  Zn_kj = (E_kj + (E Z)_kj) / (lambda_j - d_k)   (k != j)
+// and dmax = max |Zn - Z| (a non-negative double compared through its bit pattern)
+__global__ void k_sylv_update(const double2* __restrict__ E, const double2* __restrict__ EZ, const double2* __restrict__ d,
+                              const double2* __restrict__ Z, double2* __restrict__ Zn, int n, unsigned long long* __restrict__ dmax) {
+  const size_t tot = (size_t)n * n;
+  double m = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t k = i % n, j = i / n;
+    double2 v = make_double2(0, 0);
+    if (k != j) {
+      const double2 ejj = EZ[j * n + j];
+      const double2 lam = make_double2(d[j].x + ejj.x, d[j].y + ejj.y);
+      v = cdiv(make_double2(E[i].x + EZ[i].x, E[i].y + EZ[i].y), make_double2(lam.x - d[k].x, lam.y - d[k].y));
+    }
+    Zn[i] = v;
+    const double dd = fmax(fabs(v.x - Z[i].x), fabs(v.y - Z[i].y));
+    m = (dd == dd) ? fmax(m, dd) : INFINITY;      // NaN marks divergence
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(dmax, (unsigned long long)__double_as_longlong(m));
+}
+// eigenvalues lambda_j = d_j + (E Z)_jj and eigenvectors X = I + Z (in place of Z)
+__global__ void k_sylv_finish(const double2* __restrict__ EZ, const double2* __restrict__ d, double2* __restrict__ Z,
+                              double2* __restrict__ lam, int n) {
+  const size_t tot = (size_t)n * n;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t k = i % n, j = i / n;
+    if (k == j) {
+      Z[i] = make_double2(1.0, 0.0);
+      lam[j] = make_double2(d[j].x + EZ[i].x, d[j].y + EZ[i].y);
+    }
+  }
+}
+
 // ------------------------------------------------------------------ batched Lanczos (W inner product)
 // Per block b the vectors live at v + b*N etc.; scalars alpha[j*nblk+b], beta2[j*nblk+b].
 __device__ __forceinline__ uint32_t hash32(uint32_t x) {
@@ -304,6 +372,8 @@ static cx_status lanczos_bounds(cx_handle h, int K, std::vector<double>& lmin, s
 
 struct RRWork {
   double2 *G, *Hs, *V, *ev;
+  double2 *Gw, *T, *U, *B, *Z, *Zn, *EZ, *Hs0;   // subspace eigensolver (W-similarity + refinement)
+  double *wh, *dmax;
   float2 *Gf, *Mf, *Cf;
   double* scfac;
   int* perm;
@@ -312,7 +382,7 @@ struct RRWork {
 
 static cx_status rr_workspace(cx_handle h, int nmax, int ncolmax, RRWork& w) {
   const size_t n2 = (size_t)nmax * nmax;
-  const size_t need = n2 * 16 * 3 + nmax * 16 + n2 * 8 * 3 + (size_t)ncolmax * 8 + nmax * 4 + 64 + 16 * 256;
+  const size_t need = n2 * 16 * 11 + nmax * 16 + nmax * 8 + 64 + n2 * 8 * 3 + (size_t)ncolmax * 8 + nmax * 4 + 64 + 32 * 256;
   cx_status s = ensure(h, &h->d_rr, &h->rr_bytes, need);
   if (s != CX_OK) return s;
   char* p = (char*)h->d_rr;
@@ -321,6 +391,16 @@ static cx_status rr_workspace(cx_handle h, int nmax, int ncolmax, RRWork& w) {
   w.Hs = (double2*)take(n2 * 16);
   w.V = (double2*)take(n2 * 16);
   w.ev = (double2*)take(nmax * 16);
+  w.Gw = (double2*)take(n2 * 16);
+  w.T = (double2*)take(n2 * 16);
+  w.U = (double2*)take(n2 * 16);
+  w.B = (double2*)take(n2 * 16);
+  w.Z = (double2*)take(n2 * 16);
+  w.Zn = (double2*)take(n2 * 16);
+  w.EZ = (double2*)take(n2 * 16);
+  w.Hs0 = (double2*)take(n2 * 16);
+  w.wh = (double*)take(nmax * 8);
+  w.dmax = (double*)take(64);
   w.Gf = (float2*)take(n2 * 8);
   w.Mf = (float2*)take(n2 * 8);
   w.Cf = (float2*)take(n2 * 8);
@@ -361,6 +441,26 @@ cx_status rr_gemms<float>(cx_handle h, const float2* X, const float2* HX, int N,
   return CX_OK;
 }
 
+// Gw = X^H Y (complex128 result; complex64 inputs through 3xBF16 tensor-core emulation)
+static cx_status rr_gram(cx_handle h, const double2* X, const double2* Y, int N, int n, RRWork& w) {
+  const cuDoubleComplex one = make_cuDoubleComplex(1, 0), zero = make_cuDoubleComplex(0, 0);
+  CX_TRY_BLAS(h, cublasSetMathMode(h->cublas, CUBLAS_DEFAULT_MATH));
+  CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_C, CUBLAS_OP_N, n, n, N, &one, (const cuDoubleComplex*)X, N, (const cuDoubleComplex*)Y,
+                             N, &zero, (cuDoubleComplex*)w.Gw, n));
+  return CX_OK;
+}
+static cx_status rr_gram(cx_handle h, const float2* X, const float2* Y, int N, int n, RRWork& w) {
+  const cuComplex one = make_cuComplex(1, 0), zero = make_cuComplex(0, 0);
+  CX_TRY_BLAS(h, cublasSetMathMode(h->cublas, CUBLAS_FP32_EMULATED_BF16X9_MATH));
+  CX_TRY_BLAS(h, cublasSetEmulationStrategy(h->cublas, CUBLAS_EMULATION_STRATEGY_EAGER));
+  CX_TRY_BLAS(h, cublasCgemm(h->cublas, CUBLAS_OP_C, CUBLAS_OP_N, n, n, N, &one, (const cuComplex*)X, N, (const cuComplex*)Y, N, &zero,
+                             (cuComplex*)w.Gf, n));
+  const size_t n2 = (size_t)n * n;
+  k_f2d<<<grid_for(n2), 256, 0, h->stream>>>(w.Gf, w.Gw, n2);
+  h->launches++;
+  return CX_OK;
+}
+
 template <typename R>
 static cx_status rr_rotate(cx_handle h, const cplx<R>* X, cplx<R>* out, int N, int n, RRWork& w);
 
@@ -386,6 +486,143 @@ cx_status rr_rotate<float>(cx_handle h, const float2* X, float2* out, int N, int
   return CX_OK;
 }
 
+// Eigen-decomposition of the projected Hs (n x n, complex128, general) into w.ev / w.V.
+// Fast path: with Gwq = Q^H W Q = L L^H, T = L^H Hs L^-H is Hermitian up to the subspace residual
+// (the Hamiltonian is self-adjoint in the W inner product); the Hermitian eigenvectors U of
+// (T + T^H)/2 make B = U^H T U nearly diagonal, and the fixed point B X = X Lambda with X = I + Z is
+// iterated to convergence, giving the eigenpairs of Hs exactly (Y = L^-H U X).  When the iteration
+// does not converge (clustered spectrum, first steps) the general solver cusolverDnXgeev is used.
+// Returns in *used_fallback whether geev ran.
+static cx_status subspace_eig(cx_handle h, int n, RRWork& w, bool* used_fallback) {
+  const cuDoubleComplex one = make_cuDoubleComplex(1, 0), zero = make_cuDoubleComplex(0, 0);
+  const size_t n2 = (size_t)n * n;
+  const unsigned gn = grid_for(n2);
+  cudaStream_t st = h->stream;
+  *used_fallback = false;
+  CX_TRY_BLAS(h, cublasSetMathMode(h->cublas, CUBLAS_DEFAULT_MATH));
+  CX_TRY_CUDA(h, cudaMemcpyAsync(w.Hs0, w.Hs, n2 * 16, cudaMemcpyDeviceToDevice, st));
+  // L = chol(Gwq) (lower)
+  size_t wsd = 0, wsh = 0;
+  CX_TRY_SOLVER(h, cusolverDnXpotrf_bufferSize(h->cusolver, h->cusolver_params, CUBLAS_FILL_MODE_LOWER, n, CUDA_C_64F, w.Gw, n,
+                                                CUDA_C_64F, &wsd, &wsh));
+  size_t wsd2 = 0, wsh2 = 0;
+  CX_TRY_SOLVER(h, cusolverDnXsyevd_bufferSize(h->cusolver, h->cusolver_params, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n,
+                                                CUDA_C_64F, w.U, n, CUDA_R_64F, w.wh, CUDA_C_64F, &wsd2, &wsh2));
+  wsd = std::max(wsd, wsd2);
+  wsh = std::max(wsh, wsh2);
+  cx_status s;
+  if ((s = ensure(h, &h->d_ws, &h->ws_bytes, wsd + 256)) != CX_OK) return s;
+  if (h->hws_bytes < wsh + 256) {
+    cudaFreeHost(h->h_ws);
+    h->h_ws = nullptr;
+    h->hws_bytes = 0;
+    CX_TRY_CUDA(h, cudaMallocHost(&h->h_ws, wsh + 256));
+    h->hws_bytes = wsh + 256;
+  }
+  CX_TRY_SOLVER(h, cusolverDnXpotrf(h->cusolver, h->cusolver_params, CUBLAS_FILL_MODE_LOWER, n, CUDA_C_64F, w.Gw, n, CUDA_C_64F,
+                                     h->d_ws, h->ws_bytes, h->h_ws, h->hws_bytes, w.info));
+  int info = 0;
+  CX_TRY_CUDA(h, cudaMemcpyAsync(&info, w.info, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CX_TRY_CUDA(h, cudaStreamSynchronize(st));
+  bool fast = info == 0;
+  // fixed-point refinement of B X = X Lambda (B in w.B is split in place into diag -> w.ev, off-diag);
+  // returns true when converged, with lambda in w.ev and X = I + Z in w.Z
+  auto refine = [&](bool* conv) -> cx_status {
+    *conv = false;
+    k_split_diag<<<gn, 256, 0, st>>>(w.B, w.ev, w.Z, n);
+    h->launches++;
+    double prev = 1e300;
+    for (int it = 0; it < 80; ++it) {
+      CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, (const cuDoubleComplex*)w.B, n,
+                                 (const cuDoubleComplex*)w.Z, n, &zero, (cuDoubleComplex*)w.EZ, n));
+      CX_TRY_CUDA(h, cudaMemsetAsync(w.dmax, 0, 8, st));
+      k_sylv_update<<<gn, 256, 0, st>>>(w.B, w.EZ, w.ev, w.Z, w.Zn, n, (unsigned long long*)w.dmax);
+      h->launches++;
+      std::swap(w.Z, w.Zn);
+      double dm = 0;
+      CX_TRY_CUDA(h, cudaMemcpyAsync(&dm, w.dmax, 8, cudaMemcpyDeviceToHost, st));
+      CX_TRY_CUDA(h, cudaStreamSynchronize(st));
+      if (!(dm < 1e300)) return CX_OK;                       // diverged (inf / NaN)
+      if (dm < 1e-12) { *conv = true; break; }
+      if (it >= 8 && dm > 0.9 * prev) return CX_OK;          // not contracting
+      prev = dm;
+    }
+    if (!*conv) return CX_OK;
+    CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, (const cuDoubleComplex*)w.B, n,
+                               (const cuDoubleComplex*)w.Z, n, &zero, (cuDoubleComplex*)w.EZ, n));
+    k_sylv_finish<<<gn, 256, 0, st>>>(w.EZ, w.ev, w.Z, w.ev, n);
+    h->launches++;
+    return CX_OK;
+  };
+  if (fast) {
+    // T = L^H (Hs L^-H)
+    CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT, n, n, &one,
+                               (const cuDoubleComplex*)w.Gw, n, (cuDoubleComplex*)w.Hs, n));
+    CX_TRY_BLAS(h, cublasZtrmm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT, n, n, &one,
+                               (const cuDoubleComplex*)w.Gw, n, (const cuDoubleComplex*)w.Hs, n, (cuDoubleComplex*)w.T, n));
+    // tier 1: the filtered block is ordered like the previous Ritz vectors, so near self-consistency T
+    // itself is nearly diagonal -- refine directly (U = I)
+    CX_TRY_CUDA(h, cudaMemcpyAsync(w.B, w.T, n2 * 16, cudaMemcpyDeviceToDevice, st));
+    bool conv = false;
+    cx_status rs = refine(&conv);
+    if (rs != CX_OK) return rs;
+    if (conv) {
+      // eigenvectors of Hs: Y = L^-H X
+      CX_TRY_CUDA(h, cudaMemcpyAsync(w.V, w.Z, n2 * 16, cudaMemcpyDeviceToDevice, st));
+      CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT, n, n, &one,
+                                 (const cuDoubleComplex*)w.Gw, n, (cuDoubleComplex*)w.V, n));
+      return CX_OK;
+    }
+    // tier 2: Hermitian eigenvectors U of (T + T^H)/2, then refine B = U^H T U
+    k_herm_part<<<gn, 256, 0, st>>>(w.T, w.U, n);
+    h->launches++;
+    CX_TRY_SOLVER(h, cusolverDnXsyevd(h->cusolver, h->cusolver_params, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, CUDA_C_64F,
+                                       w.U, n, CUDA_R_64F, w.wh, CUDA_C_64F, h->d_ws, h->ws_bytes, h->h_ws, h->hws_bytes, w.info));
+    CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, (const cuDoubleComplex*)w.T, n,
+                               (const cuDoubleComplex*)w.U, n, &zero, (cuDoubleComplex*)w.EZ, n));
+    CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_C, CUBLAS_OP_N, n, n, n, &one, (const cuDoubleComplex*)w.U, n,
+                               (const cuDoubleComplex*)w.EZ, n, &zero, (cuDoubleComplex*)w.B, n));
+    CX_TRY_CUDA(h, cudaMemcpyAsync(&info, w.info, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CX_TRY_CUDA(h, cudaStreamSynchronize(st));
+    if (info == 0) {
+      if ((rs = refine(&conv)) != CX_OK) return rs;
+      if (conv) {
+        // eigenvectors of Hs: Y = L^-H (U X)
+        CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, (const cuDoubleComplex*)w.U, n,
+                                   (const cuDoubleComplex*)w.Z, n, &zero, (cuDoubleComplex*)w.V, n));
+        CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT, n, n, &one,
+                                   (const cuDoubleComplex*)w.Gw, n, (cuDoubleComplex*)w.V, n));
+        return CX_OK;
+      }
+    }
+  }
+  // general FP64 eigensolver on the untouched Hs
+  *used_fallback = true;
+  CX_TRY_CUDA(h, cudaMemcpyAsync(w.Hs, w.Hs0, n2 * 16, cudaMemcpyDeviceToDevice, st));
+  size_t g1 = 0, g2 = 0;
+  CX_TRY_SOLVER(h, cusolverDnXgeev_bufferSize(h->cusolver, h->cusolver_params, CUSOLVER_EIG_MODE_NOVECTOR, CUSOLVER_EIG_MODE_VECTOR, n,
+                                               CUDA_C_64F, w.Hs, n, CUDA_C_64F, w.ev, CUDA_C_64F, nullptr, n, CUDA_C_64F, w.V, n,
+                                               CUDA_C_64F, &g1, &g2));
+  if ((s = ensure(h, &h->d_ws, &h->ws_bytes, g1 + 256)) != CX_OK) return s;
+  if (h->hws_bytes < g2 + 256) {
+    cudaFreeHost(h->h_ws);
+    h->h_ws = nullptr;
+    h->hws_bytes = 0;
+    CX_TRY_CUDA(h, cudaMallocHost(&h->h_ws, g2 + 256));
+    h->hws_bytes = g2 + 256;
+  }
+  CX_TRY_SOLVER(h, cusolverDnXgeev(h->cusolver, h->cusolver_params, CUSOLVER_EIG_MODE_NOVECTOR, CUSOLVER_EIG_MODE_VECTOR, n, CUDA_C_64F,
+                                    w.Hs, n, CUDA_C_64F, w.ev, CUDA_C_64F, nullptr, n, CUDA_C_64F, w.V, n, CUDA_C_64F, h->d_ws,
+                                    h->ws_bytes, h->h_ws, h->hws_bytes, w.info));
+  CX_TRY_CUDA(h, cudaMemcpyAsync(&info, w.info, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CX_TRY_CUDA(h, cudaStreamSynchronize(st));
+  if (info != 0) {
+    h->err = "eigensolver: geev failed (info " + std::to_string(info) + ")";
+    return CX_ERR_LIB;
+  }
+  return CX_OK;
+}
+
 template <typename R>
 static cx_status rayleigh_ritz_block(cx_handle h, int b, int sel, RRWork& w, double* eig_out) {
   const int N = h->g.N, n = h->blocks[b].Ns;
@@ -393,16 +630,14 @@ static cx_status rayleigh_ritz_block(cx_handle h, int b, int sel, RRWork& w, dou
   cplx<R>* HX = (cplx<R>*)h->bufs[2 * b + (sel ^ 1)];
   cx_status s = rr_gemms<R>(h, X, HX, N, n, w);
   if (s != CX_OK) return s;
+  // W-weighted Gram (needed by the subspace eigensolver): Gw = X^H (W X), W X in the H X buffer
+  k_wscale<R><<<grid_for((size_t)N * n), 256, 0, h->stream>>>(X, HX, h->d_W, N, n);
+  h->launches++;
+  if ((s = rr_gram(h, X, HX, N, n, w)) != CX_OK) return s;
   // Cholesky G = R^H R (upper)
   size_t wsd = 0, wsh = 0;
   CX_TRY_SOLVER(h, cusolverDnXpotrf_bufferSize(h->cusolver, h->cusolver_params, CUBLAS_FILL_MODE_UPPER, n, CUDA_C_64F, w.G, n,
                                                 CUDA_C_64F, &wsd, &wsh));
-  size_t wsd2 = 0, wsh2 = 0;
-  CX_TRY_SOLVER(h, cusolverDnXgeev_bufferSize(h->cusolver, h->cusolver_params, CUSOLVER_EIG_MODE_NOVECTOR, CUSOLVER_EIG_MODE_VECTOR, n,
-                                               CUDA_C_64F, w.Hs, n, CUDA_C_64F, w.ev, CUDA_C_64F, nullptr, n, CUDA_C_64F, w.V, n,
-                                               CUDA_C_64F, &wsd2, &wsh2));
-  wsd = std::max(wsd, wsd2);
-  wsh = std::max(wsh, wsh2);
   if ((s = ensure(h, &h->d_ws, &h->ws_bytes, wsd + 256)) != CX_OK) return s;
   if (h->hws_bytes < wsh + 256) {
     cudaFreeHost(h->h_ws);
@@ -423,23 +658,22 @@ static cx_status rayleigh_ritz_block(cx_handle h, int b, int sel, RRWork& w, dou
   }
   const cuDoubleComplex one = make_cuDoubleComplex(1, 0);
   CX_TRY_BLAS(h, cublasSetMathMode(h->cublas, CUBLAS_DEFAULT_MATH));
-  // Hs = R^-H M R^-1
+  // Hs = R^-H M R^-1 and Gwq = R^-H Gw R^-1 (orthonormal basis Q = X R^-1 of the same span as orth(X))
   CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT, n, n, &one,
                              (const cuDoubleComplex*)w.G, n, (cuDoubleComplex*)w.Hs, n));
   CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
                              (const cuDoubleComplex*)w.G, n, (cuDoubleComplex*)w.Hs, n));
-  // general eigensolver (eigSolver.m:110 -- Hs is not Hermitian for Cyclix cells)
-  CX_TRY_SOLVER(h, cusolverDnXgeev(h->cusolver, h->cusolver_params, CUSOLVER_EIG_MODE_NOVECTOR, CUSOLVER_EIG_MODE_VECTOR, n, CUDA_C_64F,
-                                    w.Hs, n, CUDA_C_64F, w.ev, CUDA_C_64F, nullptr, n, CUDA_C_64F, w.V, n, CUDA_C_64F, h->d_ws,
-                                    h->ws_bytes, h->h_ws, h->hws_bytes, w.info));
+  CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT, n, n, &one,
+                             (const cuDoubleComplex*)w.G, n, (cuDoubleComplex*)w.Gw, n));
+  CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
+                             (const cuDoubleComplex*)w.G, n, (cuDoubleComplex*)w.Gw, n));
+  // eigenpairs of Hs (general; eigSolver.m:110 -- Hs is not Hermitian for Cyclix cells)
+  bool fb = false;
+  if ((s = subspace_eig(h, n, w, &fb)) != CX_OK) return s;
+  h->eig_fallbacks += fb ? 1 : 0;
   std::vector<std::complex<double>> ev(n);
   CX_TRY_CUDA(h, cudaMemcpyAsync(ev.data(), w.ev, n * 16, cudaMemcpyDeviceToHost, h->stream));
-  CX_TRY_CUDA(h, cudaMemcpyAsync(&info, w.info, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   CX_TRY_CUDA(h, cudaStreamSynchronize(h->stream));
-  if (info != 0) {
-    h->err = "eigensolver: geev of block " + std::to_string(b) + " failed (info " + std::to_string(info) + ")";
-    return CX_ERR_LIB;
-  }
   // real part, ascending sort (eigSolver.m:111-116)
   std::vector<int> perm(n);
   std::iota(perm.begin(), perm.end(), 0);
@@ -579,6 +813,12 @@ cx_status cx_eigsolver(cx_handle h, int32_t count, int32_t npl, int32_t rhoTrigg
   if (count < 1 || npl < 1) { h->err = "cx_eigsolver: need count >= 1 and npl >= 1"; return CX_ERR_ARG; }
   if (h->prec == CX_PREC_FP64) return eigsolver_T<double>(h, count, npl, rhoTrigger, EigVal, a0, bup, lambda_cutoff);
   return eigsolver_T<float>(h, count, npl, rhoTrigger, EigVal, a0, bup, lambda_cutoff);
+}
+
+cx_status cx_eig_fallback_count(cx_handle h, int64_t* count) {
+  if (!h || !count) return CX_ERR_ARG;
+  *count = h->eig_fallbacks;
+  return CX_OK;
 }
 
 cx_status cx_eigsolver_host(cx_handle h, int32_t count, int32_t npl, int32_t rhoTrigger, double* psi, double* EigVal, double* a0,

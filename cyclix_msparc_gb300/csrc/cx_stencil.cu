@@ -271,8 +271,32 @@ nl_contract_kernel(const int N, const BlockDev<R>* __restrict__ blocks, const in
 // Kleinman-Bylander apply as its own pass (used after the TMA stencil, which leaves it out):
 //   out[p, s] += alpha_b * sum_{entries e of p} Chi_e . Cp[s][seg_e][:]
 // (the scatter of src/h_nonlocal_vector_mult.m:38-42, scaled like the rest of the Chebyshev step).
-// A CTA owns one 32-point row chunk (a radial tile row that some projector ball touches) and 8 states
-// (one per warp): the chunk's entries are read once from L2 and reused by the 8 warps from L1.
+// A CTA owns one 32-point row chunk (a radial tile row that some projector ball touches) and
+// 8 warps x NSW states: each warp reads a point's entries once (16-byte loads) and accumulates them
+// into NSW states at a time, so the dependent coefficient loads of the states overlap.
+constexpr int NSW = 4;   // states per warp in nl_apply_kernel
+
+template <typename R>
+__device__ __forceinline__ void load_chi4(const R* p, R c[4]) {
+  if constexpr (sizeof(R) == 4) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    c[0] = v.x; c[1] = v.y; c[2] = v.z; c[3] = v.w;
+  } else {
+    const double2 a = *reinterpret_cast<const double2*>(p), b = *reinterpret_cast<const double2*>(p + 2);
+    c[0] = a.x; c[1] = a.y; c[2] = b.x; c[3] = b.y;
+  }
+}
+template <typename R>
+__device__ __forceinline__ void load_cp4(const cplx<R>* p, cplx<R> c[4]) {
+  if constexpr (sizeof(R) == 4) {
+    const float4 a = *reinterpret_cast<const float4*>(p), b = *reinterpret_cast<const float4*>(p + 2);
+    c[0] = make_float2(a.x, a.y); c[1] = make_float2(a.z, a.w); c[2] = make_float2(b.x, b.y); c[3] = make_float2(b.z, b.w);
+  } else {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) c[q] = p[q];
+  }
+}
+
 template <typename R>
 __global__ void __launch_bounds__(256)
 nl_apply_kernel(const int N, const int Nx, const BlockDev<R>* __restrict__ blocks, const StepScalars* __restrict__ scal,
@@ -280,29 +304,44 @@ nl_apply_kernel(const int N, const int Nx, const BlockDev<R>* __restrict__ block
                 const int32_t* __restrict__ ent_start, const int32_t* __restrict__ ent_count, const int32_t* __restrict__ ent_seg,
                 const R* __restrict__ ent_chi, const cplx<R>* __restrict__ cprime, const int nseg) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int gs = blockIdx.y * 8 + w;
-  if (gs >= nstates) return;
+  const int gs0 = (blockIdx.y * 8 + w) * NSW;
+  if (gs0 >= nstates) return;
   const int p0 = chunks[blockIdx.x];
   const int r = p0 % Nx + lane;
   if (r >= Nx) return;
   const int p = p0 + lane;
   const int e0 = ent_start[p], ne = ent_count[p];
   if (ne == 0) return;
-  const int2 bs = state_tab[gs];
-  const cplx<R>* cp = cprime + (size_t)gs * nseg * kAngMax;
-  cplx<R> acc = mk<R>((R)0, (R)0);
-  for (int e = e0; e < e0 + ne; ++e) {
-    const cplx<R>* cs = cp + (size_t)ent_seg[e] * kAngMax;
-    const R* ch = ent_chi + (size_t)e * kAngMax;
+  const int nst = min(NSW, nstates - gs0);
+  cplx<R> acc[NSW];
 #pragma unroll
-    for (int q = 0; q < kAngMax; ++q) cfma(acc, ch[q], cs[q]);
+  for (int k = 0; k < NSW; ++k) acc[k] = mk<R>((R)0, (R)0);
+  for (int e = e0; e < e0 + ne; ++e) {
+    const int sg = ent_seg[e];
+    R ch[4];
+    load_chi4<R>(ent_chi + (size_t)e * kAngMax, ch);
+#pragma unroll
+    for (int k = 0; k < NSW; ++k) {
+      if (k < nst) {
+        cplx<R> cs[4];
+        load_cp4<R>(cprime + ((size_t)(gs0 + k) * nseg + sg) * kAngMax, cs);
+#pragma unroll
+        for (int q = 0; q < kAngMax; ++q) cfma(acc[k], ch[q], cs[q]);
+      }
+    }
   }
-  const R alpha = (R)scal[bs.x].alpha;
-  cplx<R>* out = blocks[bs.x].buf[out_sel] + (size_t)bs.y * N + p;
-  cplx<R> o = *out;
-  o.x = fma(alpha, acc.x, o.x);
-  o.y = fma(alpha, acc.y, o.y);
-  *out = o;
+#pragma unroll
+  for (int k = 0; k < NSW; ++k) {
+    if (k < nst) {
+      const int2 bs = state_tab[gs0 + k];
+      const R alpha = (R)scal[bs.x].alpha;
+      cplx<R>* out = blocks[bs.x].buf[out_sel] + (size_t)bs.y * N + p;
+      cplx<R> o = *out;
+      o.x = fma(alpha, acc[k].x, o.x);
+      o.y = fma(alpha, acc[k].y, o.y);
+      *out = o;
+    }
+  }
 }
 
 template <typename R>
@@ -310,7 +349,7 @@ cudaError_t launch_nl_apply(const GridDev& g, const BlockDev<R>* blocks, const S
                             int out_sel, const int* chunks, int nchunks, const int32_t* ent_start, const int32_t* ent_count,
                             const NonlocalDev& nl, const cplx<R>* cprime, cudaStream_t st) {
   if (nchunks == 0 || nl.nseg == 0) return cudaSuccess;
-  dim3 grid((unsigned)nchunks, (unsigned)((nstates + 7) / 8));
+  dim3 grid((unsigned)nchunks, (unsigned)((nstates + 8 * NSW - 1) / (8 * NSW)));
   if (grid.y > 65535) return cudaErrorInvalidConfiguration;
   nl_apply_kernel<R><<<grid, 256, 0, st>>>(g.N, g.Nx, blocks, scal, state_tab, nstates, out_sel, chunks, ent_start, ent_count, nl.ent_seg,
                                            (const R*)nl.ent_chi, cprime, nl.nseg);

@@ -168,6 +168,11 @@ class CyclixGPU:
         check(self.lib, self.h, self.lib.cx_profile_read_apply(self.h, C.byref(ms)))
         return ms.value
 
+    def eig_fallbacks(self) -> int:
+        n = C.c_int64(0)
+        check(self.lib, self.h, self.lib.cx_eig_fallback_count(self.h, C.byref(n)))
+        return n.value
+
     def launch_count(self, reset=False) -> int:
         n = C.c_int64(0)
         check(self.lib, self.h, self.lib.cx_launch_count(self.h, C.byref(n), 1 if reset else 0))

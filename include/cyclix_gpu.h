@@ -138,6 +138,10 @@ cx_status cx_eigsolver(cx_handle h, int32_t count, int32_t npl, int32_t rhoTrigg
 cx_status cx_eigsolver_host(cx_handle h, int32_t count, int32_t npl, int32_t rhoTrigger, double* psi,
                             double* EigVal, double* a0, double* bup, double* lambda_cutoff);
 
+/* Number of subspace eigen-decompositions (since cx_create) that could not use the fast
+ * Hermitian-plus-refinement path and ran the general FP64 solver instead. */
+cx_status cx_eig_fallback_count(cx_handle h, int64_t* count);
+
 /* phi = aar(Lap_std, f, guess, tol, maxit, 0.6, 0.6, 7, 6, ...) (src/poissonSolve.m:36,
  * src/aar.m:1-74) with f = -4*pi*(rho+b) given; a Jacobi preconditioner replaces ILU.
  * phi is the initial guess when use_guess != 0 (else ones, as aar.m:51-53) and the result. */
