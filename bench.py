@@ -158,6 +158,17 @@ def cpu_baseline(S, ns_total, npl, sample_states=None, workers=None):
     return total_ms, workers, sample
 
 
+# ----------------------------------------------------------------------------- replicas
+def max_over_ranks(value: float, dist=None) -> float:
+    """Slowest rank's per-step time (the whole job finishes with it); identity on one process."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ----------------------------------------------------------------------------- GPU arms
 def gpu_step_times(S, blocks, prec, steps, warmup, npl, profile_stencil=False, ramp=6):
     from cyclix_msparc_gb300.msparc import CyclixGPU
@@ -279,9 +290,12 @@ def main():
 
     dist = None
     if world > 1:
+        # replicas: every rank runs the whole workload on its own GPU; no data-path collective
         import torch.distributed as dist_mod
         dist_mod.init_process_group("gloo")
         dist = dist_mod
+        from cyclix_msparc_gb300.msparc import select_device
+        select_device(env_int("LOCAL_RANK", 0))
     S = make_system(wl)
     blocks = block_layout(wl, S)
     hbm_peak, _, peak_kind = measured_peaks()
@@ -299,11 +313,7 @@ def main():
     g, ms_mixed, launches, ev_mixed, prof, count, bounds, fb_mixed = gpu_step_times(S, blocks, "mixed", args.steps, warmup, wl.npl,
                                                                                      profile_stencil=True, ramp=args.ramp)
     clk = clocks.stop()
-    if dist:
-        import torch
-        t = torch.tensor([ms_mixed], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_mixed = float(t.item())
+    ms_mixed = max_over_ranks(ms_mixed, dist)
     e2e_ms, h2d, d2h = e2e_host(g, count + 1, wl.npl, max(2, min(args.steps, 3)), bounds)
     g.close()
     # plain FP64 arm (same steps, fewer repetitions: it is ~5x slower)

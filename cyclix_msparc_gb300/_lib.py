@@ -20,7 +20,7 @@ PREC = {"fp64": CX_PREC_FP64, "mixed": CX_PREC_MIXED}
 EXPORTS = ["cx_create", "cx_destroy", "cx_last_error", "cx_version", "cx_set_blocks", "cx_set_veff", "cx_set_psi",
            "cx_get_psi", "cx_hpsi", "cx_chebyshev_filter", "cx_eigsolver", "cx_eigsolver_host", "cx_poisson", "cx_sync",
            "cx_timer_start", "cx_timer_stop", "cx_profile_stencil", "cx_profile_read", "cx_launch_count",
-           "cx_host_register", "cx_host_unregister", "cx_hpsi_noalloc", "cx_profile_read_apply", "cx_eig_fallback_count"]
+           "cx_host_register", "cx_host_unregister", "cx_hpsi_noalloc", "cx_profile_read_apply", "cx_eig_fallback_count", "cx_scf", "cx_refine_eigenvalues", "cx_set_device"]
 
 
 class cx_grid(C.Structure):
@@ -39,6 +39,20 @@ class cx_rc_image(C.Structure):
 class cx_atom(C.Structure):
     _fields_ = [("angnum", C.c_int32), ("n_image_rc", C.c_int32), ("gamma_Jl", C.POINTER(C.c_double)),
                 ("position", C.c_double * 3), ("rcImage", C.POINTER(cx_rc_image))]
+
+
+class cx_scf_params(C.Structure):
+    _fields_ = [("scf_tol", C.c_double), ("poisson_tol", C.c_double), ("max_scf", C.c_int32), ("min_scf", C.c_int32),
+                ("rhoTrigger", C.c_int32), ("npl", C.c_int32), ("maxit_poisson", C.c_int32), ("elec_T_type", C.c_int32),
+                ("bet", C.c_double), ("occfac", C.c_double), ("NegCharge", C.c_double), ("Eself", C.c_double),
+                ("E_corr", C.c_double), ("n_atm", C.c_int32), ("mixing_param", C.c_double),
+                ("wkpt", C.POINTER(C.c_double)), ("b", C.POINTER(C.c_double)), ("rho0", C.POINTER(C.c_double)),
+                ("refine", C.c_int32)]
+
+
+class cx_scf_result(C.Structure):
+    _fields_ = [("Etotal", C.c_double), ("lambda_f", C.c_double), ("err", C.c_double), ("n_scf", C.c_int32),
+                ("converged", C.c_int32)]
 
 
 class cx_block(C.Structure):
@@ -88,6 +102,9 @@ def load(build_if_missing: bool = True):
         "cx_hpsi_noalloc": ([h, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32], C.c_int32),
         "cx_profile_read_apply": ([h, dp], C.c_int32),
         "cx_eig_fallback_count": ([h, P(C.c_int64)], C.c_int32),
+        "cx_scf": ([h, P(cx_scf_params), dp, dp, dp, dp, P(cx_scf_result)], C.c_int32),
+        "cx_refine_eigenvalues": ([h, dp], C.c_int32),
+        "cx_set_device": ([C.c_int32], C.c_int32),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

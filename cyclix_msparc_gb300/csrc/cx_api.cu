@@ -334,6 +334,19 @@ extern "C" {
 
 const char* cx_version(void) { return "cyclix_gpu 0.1 (sm_103a)"; }
 
+cx_status cx_set_device(int32_t device) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+    g_create_err = "cx_set_device: no such device";
+    return CX_ERR_ARG;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) {
+    g_create_err = "cx_set_device: cudaSetDevice failed";
+    return CX_ERR_CUDA;
+  }
+  return CX_OK;
+}
+
 const char* cx_last_error(cx_handle h) { return h ? h->err.c_str() : g_create_err.c_str(); }
 
 cx_status cx_create(const cx_grid* grid, int32_t n_atm, const cx_atom* atoms, int32_t nspin, cx_handle* out) {

@@ -33,6 +33,12 @@ cx_status make_field_map(cx_handle h, const void* base, bool is_int, struct CUte
 // fill the block part of *set (the field maps of the handle complete it)
 cx_status build_maps(cx_handle h, const std::vector<const void*>& p0, const std::vector<const void*>& p1,
                      const std::vector<int>& Ns, void** d_maps, TmaMapSet* set);
+// AAR Poisson solve on device vectors (cx_poisson.cu)
+cx_status poisson_dev(cx_handle h, const double* d_f, double* d_phi, double tol, int32_t maxit, int32_t use_guess, int32_t* iters,
+                      double* relres_out);
+cudaError_t launch_pinv_solve(double* io, int m, cudaStream_t st);
+// FP64 Rayleigh quotients of the device-resident psi (cx_linalg.cu)
+cx_status refine_eigenvalues(cx_handle h, double* EigVal);
 // status flag of the TMA pipeline: CX_OK, or CX_ERR_CUDA with a message when a CTA timed out
 cx_status check_pipeline_status(cx_handle h);
 

@@ -166,6 +166,7 @@ struct cx_handle_s {
   void* d_lz = nullptr; size_t lz_bytes = 0;         // Lanczos vectors and scalars
   void* d_misc = nullptr; size_t misc_bytes = 0;     // column norms, permutations, status
   void* d_pois = nullptr; size_t pois_bytes = 0;     // Poisson (AAR) vectors
+  void* d_scf = nullptr; size_t scf_bytes = 0;       // SCF state (density, potentials, mixing history)
 
   // TMA path (complex64): float Veff, per-point projector entry start / count, tensor maps
   float* d_veff32 = nullptr;

@@ -802,7 +802,99 @@ void cx_free_extra(cx_handle h) {
   cudaFree(h->d_lz); h->d_lz = nullptr;
   cudaFree(h->d_misc); h->d_misc = nullptr;
   cudaFree(h->d_pois); h->d_pois = nullptr;
+  cudaFree(h->d_scf); h->d_scf = nullptr;
 }
+
+// lambda_j = Re(sum W conj(a) b) / sum W |a|^2 for column j (one CTA per column)
+__global__ void k_w_rq(const double2* __restrict__ A, const double2* __restrict__ HA, const double* __restrict__ W, int N,
+                       double* __restrict__ lam) {
+  const double2* a = A + (size_t)blockIdx.x * N;
+  const double2* b = HA + (size_t)blockIdx.x * N;
+  double num = 0, den = 0;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    num += W[i] * (a[i].x * b[i].x + a[i].y * b[i].y);
+    den += W[i] * (a[i].x * a[i].x + a[i].y * a[i].y);
+  }
+  __shared__ double r1[32], r2[32];
+  for (int o = 16; o > 0; o >>= 1) { num += __shfl_xor_sync(0xffffffffu, num, o); den += __shfl_xor_sync(0xffffffffu, den, o); }
+  if ((threadIdx.x & 31) == 0) { r1[threadIdx.x >> 5] = num; r2[threadIdx.x >> 5] = den; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double n1 = 0, d1 = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) { n1 += r1[k]; d1 += r2[k]; }
+    lam[blockIdx.x] = n1 / d1;
+  }
+}
+
+namespace cx {
+// Rayleigh quotients in FP64 of the device-resident psi of every block (see cx_refine_eigenvalues).
+cx_status refine_eigenvalues(cx_handle h, double* EigVal) {
+  const int N = h->g.N;
+  int nmax = 0;
+  for (int b = 0; b < h->nblk; ++b) nmax = std::max(nmax, h->blocks[b].Ns);
+  const int nseg = std::max(1, h->nl.nseg);
+  const size_t vec = (size_t)N * nmax * sizeof(double2);
+  // two FP64 block buffers, projector coefficients, descriptors and the quotients
+  double2 *A = nullptr, *HA = nullptr, *cp = nullptr;
+  double* lam = nullptr;
+  BlockDev<double>* d_blk = nullptr;
+  int2* d_tab = nullptr;
+  StepScalars* d_sc = nullptr;
+  double2* d_ph = nullptr;
+  cx_status s = CX_OK;
+  auto fail = [&](const char* what) { h->err = std::string("cx_refine_eigenvalues: ") + what; s = CX_ERR_NOMEM; };
+  if (cudaMalloc(&A, vec) != cudaSuccess || cudaMalloc(&HA, vec) != cudaSuccess ||
+      cudaMalloc(&cp, (size_t)nmax * nseg * kAngMax * sizeof(double2)) != cudaSuccess || cudaMalloc(&lam, nmax * 8) != cudaSuccess ||
+      cudaMalloc(&d_blk, sizeof(BlockDev<double>)) != cudaSuccess || cudaMalloc(&d_tab, nmax * sizeof(int2)) != cudaSuccess ||
+      cudaMalloc(&d_sc, sizeof(StepScalars)) != cudaSuccess || cudaMalloc(&d_ph, nseg * sizeof(double2)) != cudaSuccess)
+    fail("device buffers");
+  int off = 0;
+  for (int b = 0; s == CX_OK && b < h->nblk; ++b) {
+    const int n = h->blocks[b].Ns;
+    const void* psi = h->bufs[2 * b + h->psi_sel[0]];
+    if (h->prec == CX_PREC_FP64) {
+      if (cudaMemcpyAsync(A, psi, (size_t)N * n * 16, cudaMemcpyDeviceToDevice, h->stream) != cudaSuccess) { fail("copy"); break; }
+    } else {
+      k_f2d<<<grid_for((size_t)N * n), 256, 0, h->stream>>>((const float2*)psi, A, (size_t)N * n);
+      h->launches++;
+    }
+    std::vector<BlockDev<double>> bd;
+    make_block_devs<double>(h, std::vector<cplx<double>*>{A}, std::vector<cplx<double>*>{HA}, std::vector<int>{b}, bd);
+    bd[0].Ns = n;
+    std::vector<int2> tab(n);
+    for (int i = 0; i < n; ++i) tab[i] = make_int2(0, i);
+    const StepScalars one{1.0, 0.0, 0.0, 0.0};
+    std::vector<double2> ph = segment_phases(h, h->blocks[b]);
+    if (ph.empty()) ph.push_back(make_double2(1, 0));
+    cudaMemcpyAsync(d_blk, bd.data(), sizeof(BlockDev<double>), cudaMemcpyHostToDevice, h->stream);
+    cudaMemcpyAsync(d_tab, tab.data(), n * sizeof(int2), cudaMemcpyHostToDevice, h->stream);
+    cudaMemcpyAsync(d_sc, &one, sizeof(one), cudaMemcpyHostToDevice, h->stream);
+    cudaMemcpyAsync(d_ph, ph.data(), ph.size() * sizeof(double2), cudaMemcpyHostToDevice, h->stream);
+    const double2* saved = h->nl.seg_phase;
+    h->nl.seg_phase = d_ph;
+    s = fused_step<double>(h, d_blk, d_sc, 1, d_tab, n, 0, false, cp, true, 0.0, nullptr);
+    h->nl.seg_phase = saved;
+    if (s != CX_OK) break;
+    k_w_rq<<<n, 256, 0, h->stream>>>(A, HA, h->d_W, N, lam);
+    h->launches++;
+    if (cudaMemcpyAsync(EigVal + off, lam, n * 8, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+        cudaStreamSynchronize(h->stream) != cudaSuccess) {
+      h->err = "cx_refine_eigenvalues: copy out";
+      s = CX_ERR_CUDA;
+      break;
+    }
+    off += n;
+  }
+  cudaStreamSynchronize(h->stream);
+  cudaFree(A); cudaFree(HA); cudaFree(cp); cudaFree(lam); cudaFree(d_blk); cudaFree(d_tab); cudaFree(d_sc); cudaFree(d_ph);
+  return s;
+}
+
+cx_status eigsolver_dispatch(cx_handle h, int count, int npl, int rhoTrigger, double* EigVal, double* a0, double* bup, double* lc) {
+  if (h->prec == CX_PREC_FP64) return eigsolver_T<double>(h, count, npl, rhoTrigger, EigVal, a0, bup, lc);
+  return eigsolver_T<float>(h, count, npl, rhoTrigger, EigVal, a0, bup, lc);
+}
+}  // namespace cx
 
 extern "C" {
 
@@ -813,6 +905,12 @@ cx_status cx_eigsolver(cx_handle h, int32_t count, int32_t npl, int32_t rhoTrigg
   if (count < 1 || npl < 1) { h->err = "cx_eigsolver: need count >= 1 and npl >= 1"; return CX_ERR_ARG; }
   if (h->prec == CX_PREC_FP64) return eigsolver_T<double>(h, count, npl, rhoTrigger, EigVal, a0, bup, lambda_cutoff);
   return eigsolver_T<float>(h, count, npl, rhoTrigger, EigVal, a0, bup, lambda_cutoff);
+}
+
+cx_status cx_refine_eigenvalues(cx_handle h, double* EigVal) {
+  if (!h || !EigVal) return CX_ERR_ARG;
+  if (h->nblk < 1) { h->err = "cx_refine_eigenvalues: call cx_set_blocks first"; return CX_ERR_STATE; }
+  return cx::refine_eigenvalues(h, EigVal);
 }
 
 cx_status cx_eig_fallback_count(cx_handle h, int64_t* count) {

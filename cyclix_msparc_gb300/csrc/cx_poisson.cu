@@ -170,11 +170,12 @@ __global__ void k_pois_out(const double* xold, double* phi, int N) {
 
 }  // namespace cx
 
-using namespace cx;
+namespace cx {
 
-extern "C" cx_status cx_poisson(cx_handle h, const double* f_host, double* phi_host, double tol, int32_t maxit, int32_t use_guess,
-                                int32_t* iters, double* relres_out) {
-  if (!h || !f_host || !phi_host) return CX_ERR_ARG;
+// AAR on device vectors: f (N) given, phi (N) initial guess when use_guess and result.
+cx_status poisson_dev(cx_handle h, const double* d_f, double* d_phi, double tol, int32_t maxit, int32_t use_guess, int32_t* iters,
+                      double* relres_out) {
+  if (!h || !d_f || !d_phi) return CX_ERR_ARG;
   if (maxit < 1 || !(tol > 0)) { h->err = "cx_poisson: need maxit >= 1 and tol > 0"; return CX_ERR_ARG; }
   const int N = h->g.N, m = kAarM, p = 6;
   const double omega = 0.6, beta = 0.6;
@@ -219,8 +220,8 @@ extern "C" cx_status cx_poisson(cx_handle h, const double* f_host, double* phi_h
   CX_TRY_CUDA(h, cudaMemcpyAsync(v.tab, &tab, sizeof(tab), cudaMemcpyHostToDevice, st));
   CX_TRY_CUDA(h, cudaMemcpyAsync(v.sc, &sc, sizeof(sc), cudaMemcpyHostToDevice, st));
   CX_TRY_CUDA(h, cudaMemsetAsync(v.zero, 0, (size_t)N * 8, st));
-  CX_TRY_CUDA(h, cudaMemcpyAsync(v.f, f_host, (size_t)N * 8, cudaMemcpyHostToDevice, st));
-  if (use_guess) CX_TRY_CUDA(h, cudaMemcpyAsync(v.res, phi_host, (size_t)N * 8, cudaMemcpyHostToDevice, st));
+  CX_TRY_CUDA(h, cudaMemcpyAsync(v.f, d_f, (size_t)N * 8, cudaMemcpyDeviceToDevice, st));
+  if (use_guess) CX_TRY_CUDA(h, cudaMemcpyAsync(v.res, d_phi, (size_t)N * 8, cudaMemcpyDeviceToDevice, st));
   CX_TRY_CUDA(h, cudaMemsetAsync(v.DX, 0, (size_t)N * 8 * m, st));
   CX_TRY_CUDA(h, cudaMemsetAsync(v.DF, 0, (size_t)N * 8 * m, st));
   const cx_grid& G = h->grid;
@@ -272,9 +273,8 @@ extern "C" cx_status cx_poisson(cx_handle h, const double* f_host, double* phi_h
     count++;
   }
   // the returned iterate is x_prev of the last residual evaluation (aar.m:77)
-  k_pois_out<<<gN, 256, 0, st>>>(v.xold, v.zero, N);
+  k_pois_out<<<gN, 256, 0, st>>>(v.xold, d_phi, N);
   h->launches++;
-  CX_TRY_CUDA(h, cudaMemcpyAsync(phi_host, v.zero, (size_t)N * 8, cudaMemcpyDeviceToHost, st));
   CX_TRY_CUDA(h, cudaStreamSynchronize(st));
   if (iters) *iters = std::min(count, maxit);
   if (relres_out) *relres_out = relres;
@@ -283,4 +283,41 @@ extern "C" cx_status cx_poisson(cx_handle h, const double* f_host, double* phi_h
     return CX_ERR_NOCONV;
   }
   return CX_OK;
+}
+
+// gamma = pinv(A) v for an m x m symmetric A, on the device (io layout of k_pois_pinv)
+cudaError_t launch_pinv_solve(double* io, int m, cudaStream_t st) {
+  k_pois_pinv<<<1, 32, 0, st>>>(io, m);
+  return cudaGetLastError();
+}
+
+}  // namespace cx
+
+extern "C" cx_status cx_poisson(cx_handle h, const double* f_host, double* phi_host, double tol, int32_t maxit, int32_t use_guess,
+                                int32_t* iters, double* relres_out) {
+  if (!h || !f_host || !phi_host) return CX_ERR_ARG;
+  if (maxit < 1 || !(tol > 0)) { h->err = "cx_poisson: need maxit >= 1 and tol > 0"; return CX_ERR_ARG; }
+  const size_t N = h->g.N;
+  double *df = nullptr, *dphi = nullptr;
+  cudaError_t e1 = cudaMalloc(&df, N * 8), e2 = cudaMalloc(&dphi, N * 8);
+  if (e1 != cudaSuccess || e2 != cudaSuccess) {
+    cudaFree(df);
+    cudaFree(dphi);
+    h->err = "cx_poisson: device vectors";
+    return CX_ERR_NOMEM;
+  }
+  cx_status s = CX_OK;
+  if (cudaMemcpy(df, f_host, N * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(dphi, phi_host, N * 8, cudaMemcpyHostToDevice) != cudaSuccess) {
+    h->err = "cx_poisson: copy in";
+    s = CX_ERR_CUDA;
+  }
+  if (s == CX_OK) s = cx::poisson_dev(h, df, dphi, tol, maxit, use_guess, iters, relres_out);
+  if ((s == CX_OK || s == CX_ERR_NOCONV) && cudaMemcpy(phi_host, dphi, N * 8, cudaMemcpyDeviceToHost) != cudaSuccess) {
+    h->err = "cx_poisson: copy out";
+    s = CX_ERR_CUDA;
+  }
+  cudaFree(df);
+  cudaFree(dphi);
+  return s;
 }

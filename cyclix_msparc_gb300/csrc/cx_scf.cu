@@ -1,0 +1,396 @@
+// Self-consistent field loop on the GPU (src/scf.m:1-327, first relaxation step, nspin = 1,
+// potential mixing -- the reference defaults of src/initialization.m:1004-1040):
+//   Veff0 = phi[rho0] + Vxc[rho0];  loop: eigSolver step; occupations (Fermi level of
+//   src/occupations.m); from count >= rhoTrigger: density (src/electronDensity.m:9-12), Poisson
+//   (src/poissonSolve.m), LDA_PW Vxc (src/exchangeCorrelationPotential.m:82-106), total energy
+//   (src/evaluateTotalEnergy.m:12-93) with the Escc correction (src/scf.m:152), error
+//   ||Veff - Veff_in|| / ||Veff|| (src/scf.m:177) and Periodic-Pulay mixing (src/mixing.m:20-116).
+// All N-length arithmetic is FP64 on the device; the host only drives the loop and reads scalars.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "cx_common.h"
+
+namespace cx {
+
+constexpr double kXcRhoTol = 1e-14;   // src/initialization.m:143
+constexpr int kMixHist = 7;           // src/initialization.m:1035
+
+// Fermi level by bisection on sum_b occfac w_b sum_i occ(lambda_i) + NegCharge = 0, then the
+// occupations, Eband and Eent (src/occupations.m:1-35, src/evaluateTotalEnergy.m:13-20, 76-90).
+// One CTA.  out: [0] lambda_f, [1] Eband, [2] Eent.
+__global__ void k_occupations(const double* __restrict__ ev, const double* __restrict__ w_state, int n, double bet, double occfac,
+                              double negcharge, int fermi_dirac, double* __restrict__ occ, double* __restrict__ out) {
+  __shared__ double red[32];
+  __shared__ double lohi[2];
+  auto block_sum = [&](double v) -> double {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0;
+    if (threadIdx.x == 0) {
+      for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+      red[0] = t;
+    }
+    __syncthreads();
+    t = red[0];
+    __syncthreads();
+    return t;
+  };
+  auto occ_of = [&](double lam, double mu) -> double {
+    return fermi_dirac ? 1.0 / (1.0 + exp(bet * (lam - mu))) : 0.5 * (1.0 - erf(bet * (lam - mu)));
+  };
+  double mn = 1e300, mx = -1e300;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) { mn = fmin(mn, ev[i]); mx = fmax(mx, ev[i]); }
+  for (int o = 16; o > 0; o >>= 1) { mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o)); mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o)); }
+  __shared__ double smn[32], smx[32];
+  if ((threadIdx.x & 31) == 0) { smn[threadIdx.x >> 5] = mn; smx[threadIdx.x >> 5] = mx; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < (int)(blockDim.x >> 5); ++k) { smn[0] = fmin(smn[0], smn[k]); smx[0] = fmax(smx[0], smx[k]); }
+    lohi[0] = smn[0] - 10.0;
+    lohi[1] = smx[0] + 10.0;
+  }
+  __syncthreads();
+  for (int it = 0; it < 200; ++it) {
+    const double lo = lohi[0], hi = lohi[1];
+    const double mid = 0.5 * (lo + hi);
+    if (!(hi - lo > 2e-16 * fmax(1.0, fabs(mid)))) break;
+    double f = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) f += occfac * w_state[i] * occ_of(ev[i], mid);
+    f = block_sum(f) + negcharge;
+    if (threadIdx.x == 0) { if (f > 0) lohi[1] = mid; else lohi[0] = mid; }
+    __syncthreads();
+  }
+  const double mu = 0.5 * (lohi[0] + lohi[1]);
+  double eb = 0, ee = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double o = occ_of(ev[i], mu);
+    occ[i] = o;
+    eb += occfac * w_state[i] * ev[i] * o;
+    double ent;
+    if (fermi_dirac) {
+      ent = occfac * (1 / bet) * (o * log(o) + (1 - o) * log(1 - o));
+      if (ent != ent) ent = 0.0;
+    } else {
+      const double x = bet * (ev[i] - mu);
+      ent = -occfac * (1 / bet) * 1 / (2 * sqrt(M_PI)) * exp(-x * x);
+    }
+    ee += w_state[i] * ent;
+  }
+  eb = block_sum(eb);
+  ee = block_sum(ee);
+  if (threadIdx.x == 0) { out[0] = mu; out[1] = eb; out[2] = ee; }
+}
+
+// rho[p] (+)= fac * sum_j occ_j |psi_j[p]|^2 over the Ns columns of one block (src/electronDensity.m:9-12)
+template <typename R>
+__global__ void k_density(const cplx<R>* __restrict__ psi, int N, int Ns, const double* __restrict__ occ, double fac, int accumulate,
+                          double* __restrict__ rho) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) {
+    double acc = 0;
+    for (int j = 0; j < Ns; ++j) {
+      const cplx<R> v = psi[(size_t)j * N + p];
+      acc += occ[j] * ((double)v.x * v.x + (double)v.y * v.y);
+    }
+    rho[p] = (accumulate ? rho[p] : 0.0) + fac * acc;
+  }
+}
+
+__global__ void k_poisson_rhs(const double* __restrict__ rho, const double* __restrict__ b, double* __restrict__ f, int N) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) f[p] = -4.0 * M_PI * (rho[p] + b[p]);
+}
+
+// LDA_PW exchange-correlation (src/exchangeCorrelationPotential.m:82-106 for Vxc,
+// src/evaluateTotalEnergy.m:28-43 for the energy density), Veff = phi + Vxc, and the block
+// partial sums of: [0] ec rho_c W, [1] rho_c^(4/3) W, [2] Vxc rho_c W, [3] (b - rho) phi W,
+// [4] (Veff - Veff_in) rho W, [5] (Veff - Veff_in)^2, [6] Veff^2.
+constexpr int kNSums = 7;
+__global__ void k_xc_veff(const double* __restrict__ rho, const double* __restrict__ phi, const double* __restrict__ b,
+                          const double* __restrict__ W, const double* __restrict__ veff_in, double* __restrict__ vxc,
+                          double* __restrict__ veff, int N, double* __restrict__ partial) {
+  const double A = 0.031091, alpha1 = 0.21370, beta1 = 7.5957, beta2 = 3.5876, beta3 = 1.6382, beta4 = 0.49294;
+  const double C3 = 0.9847450218427;
+  double s[kNSums] = {0, 0, 0, 0, 0, 0, 0};
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) {
+    const double r0 = rho[p];
+    const double rc = r0 < kXcRhoTol ? kXcRhoTol : r0;
+    const double rs = cbrt(0.75 / (M_PI * rc));
+    const double srs = sqrt(rs);
+    const double Q = 2 * A * (beta1 * srs + beta2 * rs + beta3 * rs * srs + beta4 * rs * rs);
+    const double lg = log(1 + 1 / Q);
+    const double dQ = A * (beta1 / srs + 2 * beta2 + 3 * beta3 * srs + 4 * beta4 * rs);
+    const double v = -C3 * cbrt(rc) + (-2 * A * (1 + alpha1 * rs)) * lg -
+                     (rs / 3) * (-2 * A * alpha1 * lg - ((-2 * A * (1 + alpha1 * rs)) * dQ) / (Q * Q + Q));
+    const double ec = -2 * A * (1 + alpha1 * rs) * lg;
+    vxc[p] = v;
+    const double ve = phi[p] + v;
+    veff[p] = ve;
+    const double w = W[p];
+    const double d = ve - veff_in[p];
+    s[0] += ec * rc * w;
+    s[1] += rc * cbrt(rc) * w;
+    s[2] += v * rc * w;
+    s[3] += (b[p] - r0) * phi[p] * w;
+    s[4] += d * r0 * w;
+    s[5] += d * d;
+    s[6] += ve * ve;
+  }
+  __shared__ double red[kNSums][32];
+#pragma unroll
+  for (int k = 0; k < kNSums; ++k) {
+    double v = s[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < kNSums) {
+    double t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[threadIdx.x][w];
+    partial[(size_t)blockIdx.x * kNSums + threadIdx.x] = t;
+  }
+}
+
+__global__ void k_sum_partials(const double* __restrict__ partial, int nblocks, int nsums, double* __restrict__ out) {
+  // one warp per sum
+  const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (k >= nsums) return;
+  double t = 0;
+  for (int i = lane; i < nblocks; i += 32) t += partial[(size_t)i * nsums + k];
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if (lane == 0) out[k] = t;
+}
+
+// Periodic Pulay (src/mixing.m:29-46): f_k = g_k - x_k and the history columns
+__global__ void k_mix_hist(const double* __restrict__ g, const double* __restrict__ x, double* __restrict__ f, double* __restrict__ X,
+                           double* __restrict__ F, const double* __restrict__ xkm1, const double* __restrict__ fkm1, int N, int col,
+                           int store) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) {
+    const double fk = g[p] - x[p];
+    f[p] = fk;
+    if (store) {
+      X[(size_t)col * N + p] = x[p] - xkm1[p];
+      F[(size_t)col * N + p] = fk - fkm1[p];
+    }
+  }
+}
+// normal matrix F'F (m x m) and F'f (m) into io (layout of launch_pinv_solve)
+__global__ void k_mix_gram(const double* __restrict__ F, const double* __restrict__ f, int N, int m, double* __restrict__ io) {
+  const int i = blockIdx.x / (m + 1), j = blockIdx.x % (m + 1);
+  const double* a = F + (size_t)i * N;
+  const double* bb = j < m ? F + (size_t)j * N : f;
+  double s = 0;
+  for (int k = threadIdx.x; k < N; k += blockDim.x) s += a[k] * bb[k];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ double red[32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+    if (j < m) io[i * m + j] = t; else io[m * m + i] = t;
+  }
+}
+// x_{k+1} = x_k - X G + beta (f_k - F G) (Anderson, src/andersonWtdAvg.m:19-21) or x_k + beta f_k;
+// then x_{k-1} = x_k, f_{k-1} = f_k
+__global__ void k_mix_update(const double* __restrict__ X, const double* __restrict__ F, const double* __restrict__ gamma, int anderson,
+                             double beta, double* __restrict__ x, const double* __restrict__ f, double* __restrict__ xkm1,
+                             double* __restrict__ fkm1, double* __restrict__ xnew, int N, int m) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) {
+    double xw = x[p], fw = f[p];
+    if (anderson)
+      for (int k = 0; k < m; ++k) {
+        xw -= X[(size_t)k * N + p] * gamma[k];
+        fw -= F[(size_t)k * N + p] * gamma[k];
+      }
+    xkm1[p] = x[p];
+    fkm1[p] = f[p];
+    xnew[p] = xw + beta * fw;
+  }
+}
+
+__global__ void k_to_float(const double* __restrict__ a, float* __restrict__ b, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = (float)a[i];
+}
+
+struct ScfBufs {
+  double *rho, *b, *phi, *vxc, *vin, *f, *X, *F, *xkm1, *fkm1, *fk, *partial, *sums, *ev, *occ, *wst, *occout, *io;
+  int nred;
+};
+
+template <typename R>
+static cx_status density_all(cx_handle h, const ScfBufs& B, const std::vector<double>& wblk) {
+  const int N = h->g.N;
+  const unsigned gN = (unsigned)std::min(152 * 8, (N + 255) / 256);
+  int off = 0;
+  for (int b = 0; b < h->nblk; ++b) {
+    const cplx<R>* psi = (const cplx<R>*)h->bufs[2 * b + h->psi_sel[0]];
+    k_density<R><<<gN, 256, 0, h->stream>>>(psi, N, h->blocks[b].Ns, B.occ + off, 2.0 * wblk[b], b > 0 ? 1 : 0, B.rho);
+    h->launches++;
+    off += h->blocks[b].Ns;
+  }
+  CX_TRY_CUDA(h, cudaGetLastError());
+  return CX_OK;
+}
+
+cx_status eigsolver_dispatch(cx_handle h, int count, int npl, int rhoTrigger, double* EigVal, double* a0, double* bup, double* lc);
+
+}  // namespace cx
+
+using namespace cx;
+
+extern "C" cx_status cx_scf(cx_handle h, const cx_scf_params* P, double* EigVal, double* rho_out, double* Veff_out, double* hist,
+                            cx_scf_result* res) {
+  if (!h || !P || !EigVal || !res) return CX_ERR_ARG;
+  if (h->nblk < 1) { h->err = "cx_scf: call cx_set_blocks (and cx_set_psi) first"; return CX_ERR_STATE; }
+  if (h->nspin != 1) { h->err = "cx_scf: the SCF driver supports nspin = 1 (spin blocks are supported by cx_eigsolver)"; return CX_ERR_ARG; }
+  if (!P->b || !P->rho0 || !P->wkpt || P->max_scf < 1 || P->npl < 1 || !(P->scf_tol > 0) || !(P->bet > 0)) {
+    h->err = "cx_scf: need b, rho0, wkpt, max_scf >= 1, npl >= 1, scf_tol > 0, bet > 0";
+    return CX_ERR_ARG;
+  }
+  const int N = h->g.N, nblk = h->nblk, m = kMixHist;
+  const cudaStream_t st = h->stream;
+  const unsigned gN = (unsigned)std::min(152 * 8, (N + 255) / 256);
+  const int ntot = h->nstates;
+  // ---- device buffers
+  ScfBufs B{};
+  B.nred = (int)gN;
+  const size_t need = (size_t)N * 8 * (9 + 2 * m) + (size_t)gN * kNSums * 8 + 64 * 8 + (size_t)ntot * 8 * 3 + 8 * (m * m + 2 * m + 8) +
+                      64 * 256;
+  if (h->scf_bytes < need) {
+    cudaFree(h->d_scf);
+    h->d_scf = nullptr;
+    h->scf_bytes = 0;
+    CX_TRY_CUDA(h, cudaMalloc(&h->d_scf, need));
+    h->scf_bytes = need;
+  }
+  {
+    char* q = (char*)h->d_scf;
+    auto take = [&](size_t bytes) { double* o = (double*)q; q += (bytes + 255) & ~(size_t)255; return o; };
+    B.rho = take((size_t)N * 8); B.b = take((size_t)N * 8); B.phi = take((size_t)N * 8); B.vxc = take((size_t)N * 8);
+    B.vin = take((size_t)N * 8); B.f = take((size_t)N * 8); B.xkm1 = take((size_t)N * 8); B.fkm1 = take((size_t)N * 8);
+    B.fk = take((size_t)N * 8); B.X = take((size_t)N * 8 * m); B.F = take((size_t)N * 8 * m);
+    B.partial = take((size_t)gN * kNSums * 8); B.sums = take(64 * 8); B.ev = take((size_t)ntot * 8); B.occ = take((size_t)ntot * 8);
+    B.wst = take((size_t)ntot * 8); B.occout = take(8 * 8); B.io = take(8 * (m * m + 2 * m + 8));
+  }
+  std::vector<double> wblk(P->wkpt, P->wkpt + nblk), wst(ntot);
+  for (int b = 0, o = 0; b < nblk; ++b)
+    for (int j = 0; j < h->blocks[b].Ns; ++j) wst[o++] = wblk[b];
+  CX_TRY_CUDA(h, cudaMemcpyAsync(B.wst, wst.data(), ntot * 8, cudaMemcpyHostToDevice, st));
+  CX_TRY_CUDA(h, cudaMemcpyAsync(B.b, P->b, (size_t)N * 8, cudaMemcpyHostToDevice, st));
+  CX_TRY_CUDA(h, cudaMemcpyAsync(B.rho, P->rho0, (size_t)N * 8, cudaMemcpyHostToDevice, st));
+  CX_TRY_CUDA(h, cudaMemsetAsync(B.X, 0, (size_t)N * 8 * m, st));
+  CX_TRY_CUDA(h, cudaMemsetAsync(B.F, 0, (size_t)N * 8 * m, st));
+  CX_TRY_CUDA(h, cudaMemsetAsync(B.fkm1, 0, (size_t)N * 8, st));
+  CX_TRY_CUDA(h, cudaMemsetAsync(B.vin, 0, (size_t)N * 8, st));
+  const double ptol = P->poisson_tol > 0 ? P->poisson_tol : 0.01 * P->scf_tol;
+  const int pmax = P->maxit_poisson > 0 ? P->maxit_poisson : 1000;
+  double sums[kNSums];
+  auto refresh_veff = [&]() -> cx_status {
+    // the block operators read d_veff (complex128 path) and its float copy (complex64 path)
+    if (h->d_veff32) {
+      k_to_float<<<gN, 256, 0, st>>>(h->d_veff, h->d_veff32, N);
+      h->launches++;
+    }
+    CX_TRY_CUDA(h, cudaGetLastError());
+    return CX_OK;
+  };
+  auto potential = [&](int use_guess) -> cx_status {
+    // phi = Poisson(rho), Vxc(rho), Veff = phi + Vxc (into h->d_veff) and the energy / error sums
+    k_poisson_rhs<<<gN, 256, 0, st>>>(B.rho, B.b, B.f, N);
+    h->launches++;
+    int it = 0;
+    double rr = 0;
+    cx_status s = poisson_dev(h, B.f, B.phi, ptol, pmax, use_guess, &it, &rr);
+    if (s != CX_OK && s != CX_ERR_NOCONV) return s;
+    k_xc_veff<<<gN, 256, 0, st>>>(B.rho, B.phi, B.b, h->d_W, B.vin, B.vxc, h->d_veff, N, B.partial);
+    k_sum_partials<<<1, 32 * kNSums, 0, st>>>(B.partial, (int)gN, kNSums, B.sums);
+    h->launches += 2;
+    CX_TRY_CUDA(h, cudaMemcpyAsync(sums, B.sums, sizeof(sums), cudaMemcpyDeviceToHost, st));
+    CX_TRY_CUDA(h, cudaStreamSynchronize(st));
+    return CX_OK;
+  };
+  cx_status s;
+  // ---- initial potential (src/scf.m:32-39)
+  if ((s = potential(0)) != CX_OK) return s;
+  if ((s = refresh_veff()) != CX_OK) return s;
+  CX_TRY_CUDA(h, cudaMemcpyAsync(B.vin, h->d_veff, (size_t)N * 8, cudaMemcpyDeviceToDevice, st));   // Veff_temp
+  std::vector<double> a0(nblk, 0.0), bup(nblk, 0.0), lc(nblk, 0.0);
+  std::vector<double> ev(ntot, 0.0);
+  int count = 1, count_scf = 1;
+  double err = 100.0, Etot = 0.0, lam_f = 0.0;
+  const double C2 = 0.73855876638202;
+  const int rhoTrigger = P->rhoTrigger > 0 ? P->rhoTrigger : 4;
+  while ((err > P->scf_tol && count_scf <= P->max_scf) || count_scf <= P->min_scf) {
+    if ((s = eigsolver_dispatch(h, count, P->npl, rhoTrigger, ev.data(), a0.data(), bup.data(), lc.data())) != CX_OK) return s;
+    CX_TRY_CUDA(h, cudaMemcpyAsync(B.ev, ev.data(), ntot * 8, cudaMemcpyHostToDevice, st));
+    k_occupations<<<1, 1024, 0, st>>>(B.ev, B.wst, ntot, P->bet, P->occfac, P->NegCharge, P->elec_T_type == 0, B.occ, B.occout);
+    h->launches++;
+    double occout[3];
+    CX_TRY_CUDA(h, cudaMemcpyAsync(occout, B.occout, sizeof(occout), cudaMemcpyDeviceToHost, st));
+    CX_TRY_CUDA(h, cudaStreamSynchronize(st));
+    lam_f = occout[0];
+    if (count >= rhoTrigger) {
+      s = h->prec == CX_PREC_FP64 ? density_all<double>(h, B, wblk) : density_all<float>(h, B, wblk);
+      if (s != CX_OK) return s;
+      if ((s = potential(1)) != CX_OK) return s;
+      const double Exc = sums[0] - C2 * sums[1], Exc_dc = sums[2], Eelec_dc = 0.5 * sums[3], Escc = sums[4];
+      Etot = occout[1] + Exc - Exc_dc + Eelec_dc - P->Eself + P->E_corr + occout[2] + Escc;
+      err = std::sqrt(sums[5]) / std::sqrt(sums[6]);
+      if (hist && count_scf <= P->max_scf) {
+        hist[2 * (count_scf - 1)] = Etot / std::max(1, P->n_atm);
+        hist[2 * (count_scf - 1) + 1] = err;
+      }
+      if (err > P->scf_tol || count_scf < P->min_scf) {
+        // potential mixing of the mean-free Veff (the mean is 0 for non-periodic cells, src/scf.m:201-215)
+        const int col = (count_scf - 2 + m) % m;
+        k_mix_hist<<<gN, 256, 0, st>>>(h->d_veff, B.vin, B.fk, B.X, B.F, B.xkm1, B.fkm1, N, col, count_scf > 1 ? 1 : 0);
+        h->launches++;
+        const int anderson = count_scf > 1 ? 1 : 0;     // PulayFrequency = 1
+        if (anderson) {
+          k_mix_gram<<<m * (m + 1), 256, 0, st>>>(B.F, B.fk, N, m, B.io);
+          CX_TRY_CUDA(h, launch_pinv_solve(B.io, m, st));
+          h->launches += 2;
+        }
+        k_mix_update<<<gN, 256, 0, st>>>(B.X, B.F, B.io + m * m + m, anderson, P->mixing_param > 0 ? P->mixing_param : 0.3, B.vin, B.fk,
+                                         B.xkm1, B.fkm1, h->d_veff, N, m);
+        h->launches++;
+        CX_TRY_CUDA(h, cudaMemcpyAsync(B.vin, h->d_veff, (size_t)N * 8, cudaMemcpyDeviceToDevice, st));
+      }
+      if ((s = refresh_veff()) != CX_OK) return s;
+      count_scf++;
+    }
+    count++;
+    if (count > 10 * (P->max_scf + rhoTrigger)) break;
+  }
+  CX_TRY_CUDA(h, cudaStreamSynchronize(st));
+  if (P->refine && count_scf > 1) {
+    // final FP64 refinement step: Rayleigh quotients of the psi of the last step under the potential
+    // they were computed for (Veff_in), then occupations, band and entropy energy again; the
+    // density-dependent terms of the last step are kept (the energy is stationary in them)
+    CX_TRY_CUDA(h, cudaMemcpyAsync(B.f, h->d_veff, (size_t)N * 8, cudaMemcpyDeviceToDevice, st));
+    CX_TRY_CUDA(h, cudaMemcpyAsync(h->d_veff, B.vin, (size_t)N * 8, cudaMemcpyDeviceToDevice, st));
+    s = refine_eigenvalues(h, ev.data());
+    CX_TRY_CUDA(h, cudaMemcpyAsync(h->d_veff, B.f, (size_t)N * 8, cudaMemcpyDeviceToDevice, st));
+    if (s != CX_OK) return s;
+    CX_TRY_CUDA(h, cudaMemcpyAsync(B.ev, ev.data(), ntot * 8, cudaMemcpyHostToDevice, st));
+    k_occupations<<<1, 1024, 0, st>>>(B.ev, B.wst, ntot, P->bet, P->occfac, P->NegCharge, P->elec_T_type == 0, B.occ, B.occout);
+    h->launches++;
+    double occout[3];
+    CX_TRY_CUDA(h, cudaMemcpyAsync(occout, B.occout, sizeof(occout), cudaMemcpyDeviceToHost, st));
+    CX_TRY_CUDA(h, cudaStreamSynchronize(st));
+    const double Exc = sums[0] - C2 * sums[1], Exc_dc = sums[2], Eelec_dc = 0.5 * sums[3], Escc = sums[4];
+    Etot = occout[1] + Exc - Exc_dc + Eelec_dc - P->Eself + P->E_corr + occout[2] + Escc;
+    lam_f = occout[0];
+  }
+  std::copy(ev.begin(), ev.end(), EigVal);
+  if (rho_out) CX_TRY_CUDA(h, cudaMemcpy(rho_out, B.rho, (size_t)N * 8, cudaMemcpyDeviceToHost));
+  if (Veff_out) CX_TRY_CUDA(h, cudaMemcpy(Veff_out, h->d_veff, (size_t)N * 8, cudaMemcpyDeviceToHost));
+  res->Etotal = Etot;
+  res->lambda_f = lam_f;
+  res->err = err;
+  res->n_scf = count_scf - 1;
+  res->converged = err <= P->scf_tol ? 1 : 0;
+  return CX_OK;
+}

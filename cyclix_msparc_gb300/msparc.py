@@ -22,7 +22,7 @@ import numpy as np
 from . import _lib
 from ._lib import CxError, check, cptr, dptr
 
-__all__ = ["CyclixGPU", "attach", "h_nonlocal_vector_mult", "chebyshev_filter", "eigSolver", "poissonSolve", "CxError"]
+__all__ = ["CyclixGPU", "attach", "h_nonlocal_vector_mult", "chebyshev_filter", "eigSolver", "poissonSolve", "scf", "CxError"]
 
 
 class CyclixGPU:
@@ -130,6 +130,25 @@ class CyclixGPU:
                                                            cptr(psi_packed),
                                                            dptr(EigVal), dptr(a0), dptr(bup), dptr(lambda_cutoff)))
 
+    def scf(self, S, scf_tol=1e-6, poisson_tol=-1.0, max_scf=100, min_scf=3, rhoTrigger=4, maxit_poisson=1000,
+            mixing_param=0.3, refine=None):
+        """Full SCF on the device-resident psi (cx_scf); returns (result, EigVal packed, rho, Veff, history)."""
+        wk = np.ascontiguousarray([S.wkpt[i % S.tnkpt] for i in range(len(self.blocks))], dtype=np.float64)
+        b = np.ascontiguousarray(S.b, dtype=np.float64)
+        rho0 = np.ascontiguousarray(S.rho_at, dtype=np.float64)
+        p = _lib.cx_scf_params(scf_tol=scf_tol, poisson_tol=poisson_tol, max_scf=max_scf, min_scf=min_scf, rhoTrigger=rhoTrigger,
+                               npl=int(S.npl), maxit_poisson=maxit_poisson, elec_T_type=int(S.elec_T_type), bet=float(S.bet),
+                               occfac=float(S.occfac), NegCharge=float(S.NegCharge), Eself=float(S.Eself), E_corr=float(S.E_corr),
+                               n_atm=int(S.n_atm), mixing_param=mixing_param, wkpt=dptr(wk), b=dptr(b), rho0=dptr(rho0),
+                               refine=int(self.prec == "mixed" if refine is None else refine))
+        EV = np.zeros(int(sum(self.Ns)))
+        rho = np.zeros(self.N)
+        V = np.zeros(self.N)
+        hist = np.zeros((max_scf, 2))
+        res = _lib.cx_scf_result()
+        check(self.lib, self.h, self.lib.cx_scf(self.h, C.byref(p), dptr(EV), dptr(rho), dptr(V), dptr(hist), C.byref(res)))
+        return res, EV, rho, V, hist[: res.n_scf]
+
     def poisson(self, f, phi0=None, tol=1e-8, maxit=1000):
         f = np.ascontiguousarray(f, dtype=np.float64)
         phi = np.ascontiguousarray(phi0 if phi0 is not None else np.zeros(self.N), dtype=np.float64).copy()
@@ -190,6 +209,12 @@ class CyclixGPU:
             pass
 
 
+def select_device(device: int) -> None:
+    """Device of the handles this process creates next (one process per GPU)."""
+    lib = _lib.load()
+    check(lib, None, lib.cx_set_device(int(device)))
+
+
 def attach(S, blocks, prec="mixed") -> CyclixGPU:
     """Create the GPU operator for ``S`` and keep it in ``S.gpu``."""
     S.gpu = CyclixGPU(S, blocks, prec)
@@ -248,6 +273,18 @@ def eigSolver(S, count, upper_bound_guess_vecs, psi, EigVal, a0, bup, lambda_cut
         psi_out = out
         EigVal_out = EV
     return upper_bound_guess_vecs, psi_out, EigVal_out, a0, bup, lc
+
+
+def scf(S, scf_tol=1e-6):
+    """``S = scf(S)`` (src/scf.m:1-327): the whole SCF on the GPU from ``S.rho_at`` and the psi held in ``S.gpu``.
+
+    Sets ``S.Etotal``, ``S.EigVal`` (packed per block), ``S.lambda_f``, ``S.rho``, ``S.Veff`` and ``S.extra['scf']``.
+    """
+    res, EV, rho, V, hist = S.gpu.scf(S, scf_tol=scf_tol, rhoTrigger=getattr(S, "rhoTrigger", 4))
+    S.Etotal, S.EigVal, S.lambda_f, S.rho = res.Etotal, EV, res.lambda_f, rho
+    S.Veff = V.reshape(-1, 1)
+    S.extra["scf"] = dict(n_scf=res.n_scf, converged=bool(res.converged), err=res.err, history=hist)
+    return S
 
 
 def poissonSolve(S, poisson_tol, Isguess):

@@ -105,6 +105,10 @@ cx_status cx_destroy(cx_handle h);
 const char* cx_last_error(cx_handle h);
 /* Library version string. */
 const char* cx_version(void);
+/* Device of the handles the calling thread creates next (default: device 0).  One process per
+ * GPU selects its local device once before cx_create; no reference counterpart (MATLAB runs one
+ * process on one device). */
+cx_status cx_set_device(int32_t device);
 
 /* Blocks and working precision; allocates two device buffers per block
  * (psi and one work array).  Replaces any previous block set. */
@@ -159,6 +163,49 @@ cx_status cx_poisson(cx_handle h, const double* f, double* phi, double tol, int3
  * array's address and should come before any stream capture.  Calls share the array: calls
  * whose work overlaps on the GPU race.  Each call waits for its own work before returning. */
 cx_status cx_hpsi_noalloc(cx_handle h, int32_t blk, int32_t ncol, const void* X_dev, void* Y_dev, int32_t prec);
+
+/* SCF parameters: the S fields read by src/scf.m (nspin = 1, LDA_PW, potential mixing). */
+typedef struct {
+  double scf_tol;            /* S.SCF_tol: stop when ||Veff - Veff_in|| / ||Veff|| <= scf_tol */
+  double poisson_tol;        /* S.poisson_tol (<= 0: 0.01 * scf_tol, src/initialization.m:548-552) */
+  int32_t max_scf, min_scf;  /* S.MAXIT_SCF, S.MINIT_SCF */
+  int32_t rhoTrigger;        /* S.rhoTrigger (Chebyshev cycles of the first SCF step) */
+  int32_t npl;               /* S.npl */
+  int32_t maxit_poisson;     /* S.MAXIT_POISSON */
+  int32_t elec_T_type;       /* 0 Fermi-Dirac, 1 Gaussian smearing */
+  double bet;                /* S.bet (1 / smearing) */
+  double occfac;             /* S.occfac */
+  double NegCharge;          /* S.NegCharge */
+  double Eself, E_corr;      /* S.Eself, S.E_corr */
+  int32_t n_atm;             /* S.n_atm (energy per atom in hist) */
+  double mixing_param;       /* S.MixingParameter */
+  const double* wkpt;        /* k-point weight of each block (nblk) */
+  const double* b;           /* S.b, pseudocharge density (N) */
+  const double* rho0;        /* initial density (N) */
+  int32_t refine;            /* != 0: after the loop, replace the eigenvalues by FP64 Rayleigh quotients of
+                                H[Veff_in] (cx_refine_eigenvalues) and re-evaluate occupations and energy */
+} cx_scf_params;
+
+typedef struct {
+  double Etotal;             /* free energy (Ha) of the last SCF step, with Escc */
+  double lambda_f;           /* Fermi level */
+  double err;                /* last SCF error */
+  int32_t n_scf;             /* SCF steps taken */
+  int32_t converged;
+} cx_scf_result;
+
+/* S = scf(S) (src/scf.m:1-327) on the device-resident psi of the handle's blocks: initial
+ * potential from rho0, then eigSolver / occupations / density / Poisson / LDA_PW / energy /
+ * Periodic-Pulay potential mixing until converged.  EigVal (packed, sum Ns), rho (N), Veff (N)
+ * and hist (max_scf x 2: energy per atom, error per SCF step) are outputs (rho, Veff, hist may
+ * be NULL). */
+cx_status cx_scf(cx_handle h, const cx_scf_params* p, double* EigVal, double* rho, double* Veff, double* hist,
+                 cx_scf_result* res);
+
+/* FP64 refinement of the Ritz values of the device-resident psi: lambda_j = Re(psi_j^H W H psi_j) /
+ * (psi_j^H W psi_j) with H applied in complex128 (the Hamiltonian is self-adjoint in the W inner
+ * product, so the error is second order in the error of psi).  EigVal packed (sum Ns), output. */
+cx_status cx_refine_eigenvalues(cx_handle h, double* EigVal);
 
 /* ---- measurement -------------------------------------------------------- */
 /* Wait for all work of h. */

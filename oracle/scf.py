@@ -1,0 +1,220 @@
+"""Oracle restatement of the SCF bookkeeping around the CheFSI path.
+
+Test infrastructure only (see ``oracle/__init__.py``).  Paths relative to the reference project
+root ``Cyclix_MS_200220/``.  Covers the non-spin LDA_PW potential-mixing SCF of src/scf.m with the
+reference defaults (MixingVariable = 1, MixingPrecond = 0, PulayFrequency = 1, MixingHistory = 7,
+MixingParameter = 0.3, rhoTrigger = 4, MINIT_SCF = 3; src/initialization.m:1004-1040).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import scipy.linalg as sla
+import scipy.optimize as so
+import scipy.sparse.linalg as spla
+from scipy.special import erf
+
+from . import cychel_ops as O
+
+XC_RHOTOL = 1e-14   # src/initialization.m:143
+
+
+# ---------------------------------------------------------------------------------------------
+# src/aar.m:1-74 with the ILU(1e-5) preconditioner of src/initialization.m:752
+# ---------------------------------------------------------------------------------------------
+def aar(A, b, x_guess, tol, max_iter, omega, beta, m, p, M_solve):
+    N = b.shape[0]
+    DX = np.zeros((N, m))
+    DF = np.zeros((N, m))
+    nb = 1 / np.linalg.norm(b)
+    x_prev = np.ones(N) if x_guess is None else x_guess.copy()
+    relres = 1 + tol
+    count = 1
+    x = x_prev
+    Xold = Fold = None
+    while count <= max_iter and relres > tol:
+        res1 = b - A @ x_prev
+        relres = np.linalg.norm(res1) * nb
+        res = M_solve(res1)
+        if count > 1:
+            DX[:, (count - 2) % m] = x_prev - Xold
+            DF[:, (count - 2) % m] = res - Fold
+        Xold = x_prev
+        Fold = res
+        if count % p != 0:
+            x_new = x_prev + omega * res
+        else:
+            x_new = x_prev + beta * res - (DX + beta * DF) @ (np.linalg.pinv(DF.T @ DF) @ (DF.T @ res))
+        x = x_prev
+        x_prev = x_new
+        count += 1
+    return x, relres, count - 1
+
+
+class PoissonOperator:
+    """Lap_std and its ILU factors (src/initialization.m:734-752)."""
+
+    def __init__(self, S):
+        self.L = O.lap_std(S).tocsc()
+        self.ilu = spla.spilu(self.L, drop_tol=1e-5)
+
+    def solve(self, f, guess, tol, maxit=1000):
+        # src/poissonSolve.m:36: aar(Lap_std, f, guess, tol, MAXIT_POISSON, 0.6, 0.6, 7, 6, L, U)
+        return aar(self.L, f, guess, tol, maxit, 0.6, 0.6, 7, 6, self.ilu.solve)
+
+
+# ---------------------------------------------------------------------------------------------
+# src/exchangeCorrelationPotential.m:82-106 (LDA_PW potential) and
+# src/evaluateTotalEnergy.m:28-43 (LDA_PW energy)
+# ---------------------------------------------------------------------------------------------
+def lda_pw_potential(rho):
+    rho = np.where(rho < XC_RHOTOL, XC_RHOTOL, rho)
+    p, A, alpha1 = 1, 0.031091, 0.21370
+    beta1, beta2, beta3, beta4 = 7.5957, 3.5876, 1.6382, 0.49294
+    C3 = 0.9847450218427
+    rs = (0.75 / (np.pi * rho)) ** (1 / 3)
+    Q = 2 * A * (beta1 * rs ** 0.5 + beta2 * rs + beta3 * rs ** 1.5 + beta4 * rs ** (p + 1))
+    V = -C3 * rho ** (1 / 3) + (-2 * A * (1 + alpha1 * rs)) * np.log(1 + 1 / Q) \
+        - (rs / 3) * (-2 * A * alpha1 * np.log(1 + 1 / Q)
+                      - ((-2 * A * (1 + alpha1 * rs)) * (A * (beta1 * rs ** -0.5 + 2 * beta2 + 3 * beta3 * rs ** 0.5
+                                                               + 2 * (p + 1) * beta4 * rs ** p)))
+                      / (Q * Q + Q))
+    return V
+
+
+def lda_pw_energy(rho, W):
+    rho = np.where(rho < XC_RHOTOL, XC_RHOTOL, rho)
+    C2 = 0.73855876638202
+    p, A, alpha1 = 1, 0.031091, 0.21370
+    beta1, beta2, beta3, beta4 = 7.5957, 3.5876, 1.6382, 0.49294
+    rs = (0.75 / (np.pi * rho)) ** (1 / 3)
+    ec = -2 * A * (1 + alpha1 * rs) * np.log(1 + 1 / (2 * A * (beta1 * rs ** 0.5 + beta2 * rs + beta3 * rs ** 1.5
+                                                               + beta4 * rs ** (p + 1.0))))
+    return float(np.sum(ec * rho * W) - C2 * np.sum(rho ** (4 / 3) * W))
+
+
+# ---------------------------------------------------------------------------------------------
+# src/occupations.m:1-35 (Gaussian smearing, elec_T_type = 1) and src/electronDensity.m:9-12
+# ---------------------------------------------------------------------------------------------
+def occupations(EigVals, wkpt, bet, occfac, NegCharge):
+    def f(lf):
+        s = 0.0
+        for k, ev in enumerate(EigVals):
+            s += occfac * np.sum(wkpt[k] * 0.5 * (1.0 - erf(bet * (ev - lf))))
+        return s + NegCharge
+    lo, hi = min(ev.min() for ev in EigVals) - 10.0, max(ev.max() for ev in EigVals) + 10.0
+    lam_f = so.brentq(f, lo, hi, xtol=1e-15, rtol=4 * np.finfo(float).eps, maxiter=500)
+    occ = [0.5 * (1.0 - erf(bet * (ev - lam_f))) for ev in EigVals]
+    return lam_f, occ
+
+
+def electron_density(psis, occ, wkpt, N):
+    rho = np.zeros(N)
+    for k, psi in enumerate(psis):
+        rho += 2 * wkpt[k] * np.sum((psi * np.conj(psi)).real * occ[k][None, :], axis=1)
+    return rho
+
+
+# ---------------------------------------------------------------------------------------------
+# src/evaluateTotalEnergy.m:12-93 (nspin = 1, LDA_PW, Gaussian smearing)
+# ---------------------------------------------------------------------------------------------
+def total_energy(EigVals, occ, wkpt, occfac, bet, lam_f, rho, b, phi, Vxc, W, Eself, E_corr):
+    Eband = sum(occfac * wkpt[k] * np.sum(EigVals[k] * occ[k]) for k in range(len(EigVals)))
+    Exc = lda_pw_energy(rho, W)
+    rho_c = np.where(rho < XC_RHOTOL, XC_RHOTOL, rho)
+    Exc_dc = float(np.sum(Vxc * rho_c * W))
+    Eelec_dc = 0.5 * float(np.sum((b - rho) * phi * W))
+    Eent = 0.0
+    for k in range(len(EigVals)):
+        Eent_v = -occfac * (1 / bet) * 1 / (2 * np.sqrt(np.pi)) * np.exp(-(bet * (EigVals[k] - lam_f)) ** 2)
+        Eent += wkpt[k] * np.sum(Eent_v)
+    Etot = Eband + Exc - Exc_dc + Eelec_dc - Eself + E_corr + Eent
+    return Etot, dict(Eband=Eband, Exc=Exc, Exc_dc=Exc_dc, Eelec_dc=Eelec_dc, Eent=Eent)
+
+
+# ---------------------------------------------------------------------------------------------
+# src/mixing.m:20-116 (Periodic Pulay, no preconditioner) and src/andersonWtdAvg.m:1-23
+# ---------------------------------------------------------------------------------------------
+class PeriodicPulay:
+    def __init__(self, N, m=7, beta=0.3, omega=0.3, p=1):
+        self.X = np.zeros((N, m))
+        self.F = np.zeros((N, m))
+        self.m, self.beta, self.omega, self.p = m, beta, omega, p
+        self.fkm1 = np.zeros(N)
+        self.xkm1 = None
+
+    def __call__(self, g_k, x_k, it):
+        f_k = g_k - x_k
+        if it > 1:
+            i_hist = (it - 2) % self.m
+            self.X[:, i_hist] = x_k - self.xkm1
+            self.F[:, i_hist] = f_k - self.fkm1
+        if it % self.p == 0 and it > 1:
+            Gamma = np.linalg.pinv(self.F.T @ self.F) @ (self.F.T @ f_k)
+            x_wavg = x_k - self.X @ Gamma
+            f_wavg = f_k - self.F @ Gamma
+        else:
+            x_wavg, f_wavg = x_k, f_k
+        x_kp1 = x_wavg + (self.beta if it % self.p == 0 else self.omega) * f_wavg
+        self.fkm1 = f_k
+        self.xkm1 = x_k
+        return x_kp1
+
+
+# ---------------------------------------------------------------------------------------------
+# src/scf.m:1-327 (first relaxation step, nspin = 1, potential mixing)
+# ---------------------------------------------------------------------------------------------
+def scf(S, psis, blocks, scf_tol=1e-6, poisson_tol=None, rhoTrigger=4, max_scf=100, min_scf=3, bounds=None, log=None):
+    """Run the reference SCF on the CPU.  ``psis``: initial psi per block; ``blocks``: (kvec, spin, Ns).
+
+    ``bounds``: optional per-block (a0, bup) for the first eigSolver call instead of eigs.
+    Returns a dict with Etotal, EigVal (list), lambda_f, rho, Veff, n_scf, history.
+    """
+    N = S.N
+    poisson_tol = poisson_tol if poisson_tol is not None else 0.01 * scf_tol
+    P = PoissonOperator(S)
+    wk = np.asarray(S.wkpt)
+    rho = S.rho_at.copy()
+    phi, _, _ = P.solve(-4 * np.pi * (rho + S.b), None, poisson_tol)
+    Vxc = lda_pw_potential(rho)
+    Veff = phi + Vxc
+    mixer = PeriodicPulay(N)
+    Veff_temp = Veff.copy()
+    psis = [p.copy() for p in psis]
+    nblk = len(blocks)
+    EigVal = [np.zeros(n) for (_, _, n) in blocks]
+    a0 = np.zeros(nblk)
+    bup = np.zeros(nblk)
+    count, count_scf, err = 1, 1, 100.0
+    hist = []
+    Etot = None
+    while (err > scf_tol and count_scf <= max_scf) or count_scf <= min_scf:
+        for b_, (k, spin, n) in enumerate(blocks):
+            H = O.Hamiltonian(S, k, Veff)
+            if count == 1:
+                if bounds is not None:
+                    bup[b_], a0[b_] = bounds[b_][1], bounds[b_][0]
+                else:
+                    bup[b_], a0[b_], _ = O.spectral_bounds(H, N, b_ + 1)
+            psis[b_], EigVal[b_], (a0[b_], bup[b_], _) = O.eig_solver_block(S, H, psis[b_], count, (a0[b_], bup[b_], 0.0),
+                                                                              EigVal[b_], rhoTrigger=rhoTrigger)
+        lam_f, occ = occupations(EigVal, wk, S.bet, S.occfac, S.NegCharge)
+        if count >= rhoTrigger:
+            rho = electron_density(psis, occ, wk, N)
+            phi, _, _ = P.solve(-4 * np.pi * (rho + S.b), phi, poisson_tol)
+            Vxc = lda_pw_potential(rho)
+            Veff = phi + Vxc
+            Etot, parts = total_energy(EigVal, occ, wk, S.occfac, S.bet, lam_f, rho, S.b, phi, Vxc, S.W, S.Eself, S.E_corr)
+            Escc = float(np.sum((Veff - Veff_temp) * rho * S.W))
+            Etot += Escc
+            err = np.linalg.norm(Veff - Veff_temp) / np.linalg.norm(Veff)
+            hist.append((count_scf, Etot / S.n_atm, err))
+            if log:
+                log(count_scf, Etot / S.n_atm, err)
+            if err > scf_tol or count_scf < min_scf:
+                Veff = mixer(Veff, Veff_temp, count_scf)
+                Veff_temp = Veff.copy()
+            count_scf += 1
+        count += 1
+    return dict(Etotal=Etot, EigVal=EigVal, lambda_f=lam_f, rho=rho, Veff=Veff, n_scf=count_scf - 1, history=hist, psis=psis)

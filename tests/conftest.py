@@ -6,8 +6,9 @@ import numpy as np
 import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
-if str(ROOT) not in sys.path:
-    sys.path.insert(0, str(ROOT))
+for _p in (ROOT, ROOT / "tests"):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
 
 
 def pytest_configure(config):
@@ -54,7 +55,14 @@ def small_helical():
 @pytest.fixture(scope="session")
 def tiny_helical():
     """A tiny helical cell whose dense Hamiltonian is cheap (1280 points, 2 atoms, 2 blocks)."""
-    from cyclix_msparc_gb300.workloads import Workload, make_system
-    wl = Workload("helical-tiny-16x8x10", 16, 8, 10, (6, 6), ((0.0, 1.0, 0.0), (0.0, 0.0, 0.9)), 1, 6, 2, 4,
-                  twist=0.05, L1=4.0, xin=4.0)
-    return make_system(wl)
+    from cyclix_msparc_gb300.workloads import make_system
+    from kat_systems import tiny_helical_workload
+    return make_system(tiny_helical_workload())
+
+
+@pytest.fixture(scope="session")
+def tiny_cyclic():
+    """A tiny cyclic cell (1280 points, 2 atoms, one block nu = 1, eta = 0.9)."""
+    from cyclix_msparc_gb300.workloads import make_system
+    from kat_systems import tiny_cyclic_workload
+    return make_system(tiny_cyclic_workload())
