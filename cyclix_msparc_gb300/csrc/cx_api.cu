@@ -205,11 +205,13 @@ cx_status build_maps(cx_handle h, const std::vector<const void*>& p0, const std:
                      void** d_maps, TmaMapSet* set) {
   *d_maps = nullptr;
   const size_t nb = p0.size();
-  std::vector<CUtensorMap_st> maps(4 * nb);
+  // [nb][2] staged-row maps, then [nb][2] theta-halo maps, then [nb][2] output-tile maps
+  std::vector<CUtensorMap_st> maps(6 * nb);
   for (size_t b = 0; b < nb; ++b) {
-    cx_status s = make_buffer_maps(h, p0[b], Ns[b], &maps[2 * b], &maps[2 * nb + 2 * b]);
+    cx_status s = make_buffer_maps(h, p0[b], Ns[b], &maps[2 * b], &maps[2 * nb + 2 * b], &maps[4 * nb + 2 * b]);
     if (s != CX_OK) return s;
-    if ((s = make_buffer_maps(h, p1[b], Ns[b], &maps[2 * b + 1], &maps[2 * nb + 2 * b + 1])) != CX_OK) return s;
+    if ((s = make_buffer_maps(h, p1[b], Ns[b], &maps[2 * b + 1], &maps[2 * nb + 2 * b + 1], &maps[4 * nb + 2 * b + 1])) != CX_OK)
+      return s;
   }
   void* d = nullptr;
   cudaError_t e = cudaMalloc(&d, maps.size() * sizeof(CUtensorMap_st));
@@ -218,7 +220,8 @@ cx_status build_maps(cx_handle h, const std::vector<const void*>& p0, const std:
   if (e != cudaSuccess) { cudaFree(d); h->err = std::string("tensor maps: ") + cudaGetErrorString(e); return CX_ERR_CUDA; }
   *d_maps = d;
   set->xmaps = d;
-  set->omaps = (const CUtensorMap_st*)d + 2 * nb;
+  set->hmaps = (const CUtensorMap_st*)d + 2 * nb;
+  set->omaps = (const CUtensorMap_st*)d + 4 * nb;
   set->vmaps = h->d_fmaps;
   return CX_OK;
 }

@@ -27,7 +27,8 @@ cx_status filter_blocks(cx_handle h, const BlockDev<R>* d_blocks, int nblk, cons
                         size_t total_elems, int sel0, int m, const std::vector<double>& a, const std::vector<double>& b,
                         const std::vector<double>& a0, cplx<R>* cprime, int* sel_out, const void* maps = nullptr);
 // tensor maps of one complex64 buffer of Ns states / of a 4-byte grid field (cx_stencil_tma.cu)
-cx_status make_buffer_maps(cx_handle h, const void* base, int Ns, struct CUtensorMap_st* xmap, struct CUtensorMap_st* omap);
+cx_status make_buffer_maps(cx_handle h, const void* base, int Ns, struct CUtensorMap_st* xmap, struct CUtensorMap_st* hmap,
+                           struct CUtensorMap_st* omap);
 cx_status make_field_map(cx_handle h, const void* base, bool is_int, struct CUtensorMap_st* out);
 // build the X / output maps of device buffers p0/p1 of a block set into a new device array and
 // fill the block part of *set (the field maps of the handle complete it)

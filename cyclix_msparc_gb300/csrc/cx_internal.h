@@ -101,7 +101,8 @@ cudaError_t launch_nl_contract(const GridDev& g, const BlockDev<R>* blocks, cons
 // ---------------------------------------------------------------- TMA path (cx_stencil_tma.cu)
 // Device arrays of tensor maps used by one launch of the TMA kernel.
 struct TmaMapSet {
-  const void* xmaps;         // [block][buffer] complex64 X maps (staged tile box)
+  const void* xmaps;         // [block][buffer] complex64 X maps (staged tile rows)
+  const void* hmaps;         // [block][buffer] complex64 theta-halo maps
   const void* omaps;         // [block][buffer] complex64 output-tile maps
   const void* vmaps;         // [spin] float Veff maps
 };
@@ -175,7 +176,7 @@ struct cx_handle_s {
   int* d_chunks = nullptr;                           // 32-point row chunks touched by a projector ball
   int nchunks = 0;
   void* d_fmaps = nullptr;                           // [nspin] Veff maps
-  void* d_maps = nullptr;                            // block buffers: [nblk][2] X maps, then [nblk][2] output maps
+  void* d_maps = nullptr;                            // block buffers: [nblk][2] X, halo and output maps
   cx::TmaMapSet tma_main{};
   bool tma_ok = false;                               // operator eligible for the TMA kernel
   int* d_status = nullptr;
