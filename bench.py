@@ -123,13 +123,25 @@ def cpu_baseline(S, ns_total, npl, sample_states=None, workers=None):
     import multiprocessing as mp
     import scipy.linalg as sla
     workers = workers or os.cpu_count() or 1
-    sample_states = sample_states or max(workers, 16)
+    sample_states = sample_states or max(2 * workers, 32)
     per = max(1, sample_states // workers)
     sample_states = per * workers
     k = S.kptgrid[0]
     ctx = mp.get_context("spawn")
-    with ctx.Pool(workers) as pool:
-        ts = pool.map(_cpu_hpsi_chunk, [(i, per, tuple(k), 0, S) for i in range(workers)])
+    # one BLAS thread per worker process: the workers already cover every core, and many
+    # small products per H*psi make oversubscribed BLAS threads spin against one another
+    saved = {v: os.environ.get(v) for v in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")}
+    for v in saved:
+        os.environ[v] = "1"
+    try:
+        with ctx.Pool(workers) as pool:
+            ts = pool.map(_cpu_hpsi_chunk, [(i, per, tuple(k), 0, S) for i in range(workers)])
+    finally:
+        for v, old_v in saved.items():
+            if old_v is None:
+                os.environ.pop(v, None)
+            else:
+                os.environ[v] = old_v
     t_h = max(ts)                                    # wall time of one parallel H*psi over the sample
     t_filter = t_h * (npl + 1) * (ns_total / sample_states)
     ncols = min(64, ns_total)

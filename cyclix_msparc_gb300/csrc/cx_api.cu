@@ -140,8 +140,8 @@ cx_status fused_step(cx_handle h, const BlockDev<R>* d_blocks, const StepScalars
   h->launches++;
   if (h->prof) CX_TRY_CUDA(h, cudaEventRecord(h->ev1, h->stream));
   if (tma && nlp) {
-    CX_TRY_CUDA(h, launch_nl_apply<R>(h->g, d_blocks, d_scal, d_state_tab, nstates, in_sel ^ 1, h->d_chunks, h->nchunks,
-                                      h->d_ent_start, h->d_ent_count, *nlp, cprime, h->stream));
+    CX_TRY_CUDA(h, launch_nl_apply<R>(h->g, d_blocks, d_scal, d_state_tab, nstates, in_sel ^ 1,
+                                      sizeof(R) == 4 ? h->chunks32 : h->chunks64, cprime, nlp->nseg, h->stream));
     h->launches++;
   }
   if (h->prof) {
@@ -495,21 +495,47 @@ cx_status cx_create(const cx_grid* grid, int32_t n_atm, const cx_atom* atoms, in
   // TMA path: per-point entry start / count, float Veff and the field maps
   h->tma_ok = tma_eligible(h->g, sizeof(float2));
   if (h->tma_ok) {
-    std::vector<int32_t> est(row_ptr.begin(), row_ptr.end() - 1), ecnt(N);
-    for (int p = 0; p < N; ++p) ecnt[p] = row_ptr[p + 1] - row_ptr[p];
-    std::vector<int> chunks;
+    // 32-point row chunks that projector balls touch, each with its segments and dense Chi
+    std::vector<int32_t> cp0, cseg_ptr(1, 0), csegs;
+    std::vector<int64_t> cchi_ptr;
+    std::vector<double> cchi;
+    int kmax = 0;
     for (int row = 0; row < N / G.Nx; ++row)
       for (int r0 = 0; r0 < G.Nx; r0 += 32) {
-        const int p0 = row * G.Nx + r0;
-        if (row_ptr[std::min(p0 + 32, (row + 1) * G.Nx)] > row_ptr[p0]) chunks.push_back(p0);
+        const int p0 = row * G.Nx + r0, p1 = std::min(p0 + 32, (row + 1) * G.Nx);
+        if (row_ptr[p1] == row_ptr[p0]) continue;
+        std::vector<int32_t> sg;
+        for (int e = row_ptr[p0]; e < row_ptr[p1]; ++e) sg.push_back(ent_seg[e]);
+        std::sort(sg.begin(), sg.end());
+        sg.erase(std::unique(sg.begin(), sg.end()), sg.end());
+        const int K = (int)sg.size() * kAngMax;
+        kmax = std::max(kmax, K);
+        cp0.push_back(p0);
+        csegs.insert(csegs.end(), sg.begin(), sg.end());
+        cseg_ptr.push_back((int32_t)csegs.size());
+        cchi_ptr.push_back((int64_t)cchi.size());
+        const size_t base = cchi.size();
+        cchi.resize(base + (size_t)K * 32, 0.0);
+        for (int p = p0; p < p1; ++p)
+          for (int e = row_ptr[p]; e < row_ptr[p + 1]; ++e) {
+            const int ls = (int)(std::lower_bound(sg.begin(), sg.end(), ent_seg[e]) - sg.begin());
+            for (int q = 0; q < kAngMax; ++q) cchi[base + (size_t)(ls * kAngMax + q) * 32 + (p - p0)] = ent_chi[(size_t)e * kAngMax + q];
+          }
       }
-    h->nchunks = (int)chunks.size();
-    if ((s = upload(h, &h->d_chunks, chunks)) || (s = upload(h, &h->d_ent_start, est)) || (s = upload(h, &h->d_ent_count, ecnt)) ||
+    std::vector<float> cchi32(cchi.begin(), cchi.end());
+    int32_t *d_cp0, *d_csp, *d_csg;
+    int64_t* d_ccp;
+    double* d_cc64;
+    float* d_cc32;
+    if ((s = upload(h, &d_cp0, cp0)) || (s = upload(h, &d_csp, cseg_ptr)) || (s = upload(h, &d_csg, csegs)) ||
+        (s = upload(h, &d_ccp, cchi_ptr)) || (s = upload(h, &d_cc64, cchi)) || (s = upload(h, &d_cc32, cchi32)) ||
         (s = dalloc(h, &h->d_veff32, (size_t)N * nspin))) {
       g_create_err = h->err;
       cx_destroy(h);
       return s;
     }
+    h->chunks32 = ChunkTables{(int32_t)cp0.size(), kmax, d_cp0, d_csp, d_csg, d_ccp, d_cc32};
+    h->chunks64 = ChunkTables{(int32_t)cp0.size(), kmax, d_cp0, d_csp, d_csg, d_ccp, d_cc64};
     CX_TRY_CUDA(h, cudaMemset(h->d_veff32, 0, sizeof(float) * (size_t)N * nspin));
     std::vector<CUtensorMap_st> fm(nspin);
     for (int sp = 0; sp < nspin; ++sp)

@@ -90,10 +90,19 @@ cudaError_t launch_cheb_step(const GridDev& g, const StencilCoef& coef, const Bl
                              const StepScalars* scal, int nblk, const int2* state_tab, int nstates,
                              int in_sel, bool use_xprev, const NonlocalDev* nl, const cplx<R>* cprime,
                              cudaStream_t st);
+// 32-point row chunks touched by projector balls, with the dense Chi of each chunk
+// (32 points x K = 4 x the chunk's segments, stored [K][32], zero outside the balls).
+struct ChunkTables {
+  int32_t nchunks, kmax;
+  const int32_t* p0;          // first grid point of the chunk
+  const int32_t* seg_ptr;     // nchunks + 1
+  const int32_t* segs;        // segment ids of each chunk
+  const int64_t* chi_ptr;     // offset of the chunk's Chi block (elements)
+  const void* chi;            // float or double, per precision
+};
 template <typename R>
 cudaError_t launch_nl_apply(const GridDev& g, const BlockDev<R>* blocks, const StepScalars* scal, const int2* state_tab, int nstates,
-                            int out_sel, const int* chunks, int nchunks, const int32_t* ent_start, const int32_t* ent_count,
-                            const NonlocalDev& nl, const cplx<R>* cprime, cudaStream_t st);
+                            int out_sel, const ChunkTables& ct, const cplx<R>* cprime, int nseg, cudaStream_t st);
 template <typename R>
 cudaError_t launch_nl_contract(const GridDev& g, const BlockDev<R>* blocks, const int2* state_tab, int nstates,
                                int in_sel, const NonlocalDev& nl, cplx<R>* cprime, cudaStream_t st);
@@ -171,10 +180,7 @@ struct cx_handle_s {
 
   // TMA path (complex64): float Veff, per-point projector entry start / count, tensor maps
   float* d_veff32 = nullptr;
-  int32_t* d_ent_start = nullptr;
-  int32_t* d_ent_count = nullptr;
-  int* d_chunks = nullptr;                           // 32-point row chunks touched by a projector ball
-  int nchunks = 0;
+  cx::ChunkTables chunks32{}, chunks64{};           // projector chunks (complex64 / complex128 Chi)
   void* d_fmaps = nullptr;                           // [nspin] Veff maps
   void* d_maps = nullptr;                            // block buffers: [nblk][2] X, halo and output maps
   cx::TmaMapSet tma_main{};

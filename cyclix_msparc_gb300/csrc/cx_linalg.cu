@@ -118,7 +118,9 @@ __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
 // one fixed-point sweep of B X = X Lambda with X = I + Z (Z zero on the diagonal), B = diag(d) + E:
 //   lambda_j = d_j + (E Z)_jj ,  Zn_kj = (E_kj + (E Z)_kj) / (lambda_j - d_k)   (k != j)
 // and dmax = max |Zn - Z| (a non-negative double compared through its bit pattern)
-__global__ void k_sylv_update(const double2* __restrict__ E, const double2* __restrict__ EZ, const double2* __restrict__ d,
+// (EZ in complex128, or in complex64 from the FP32-accurate tensor-core product of the mixed path)
+template <typename V>
+__global__ void k_sylv_update(const double2* __restrict__ E, const V* __restrict__ EZ, const double2* __restrict__ d,
                               const double2* __restrict__ Z, double2* __restrict__ Zn, int n, unsigned long long* __restrict__ dmax) {
   const size_t tot = (size_t)n * n;
   double m = 0;
@@ -126,9 +128,9 @@ __global__ void k_sylv_update(const double2* __restrict__ E, const double2* __re
     const size_t k = i % n, j = i / n;
     double2 v = make_double2(0, 0);
     if (k != j) {
-      const double2 ejj = EZ[j * n + j];
-      const double2 lam = make_double2(d[j].x + ejj.x, d[j].y + ejj.y);
-      v = cdiv(make_double2(E[i].x + EZ[i].x, E[i].y + EZ[i].y), make_double2(lam.x - d[k].x, lam.y - d[k].y));
+      const V ejj = EZ[j * n + j];
+      const double2 lam = make_double2(d[j].x + (double)ejj.x, d[j].y + (double)ejj.y);
+      v = cdiv(make_double2(E[i].x + (double)EZ[i].x, E[i].y + (double)EZ[i].y), make_double2(lam.x - d[k].x, lam.y - d[k].y));
     }
     Zn[i] = v;
     const double dd = fmax(fabs(v.x - Z[i].x), fabs(v.y - Z[i].y));
@@ -527,23 +529,48 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, bool* used_fallback
   bool fast = info == 0;
   // fixed-point refinement of B X = X Lambda (B in w.B is split in place into diag -> w.ev, off-diag);
   // returns true when converged, with lambda in w.ev and X = I + Z in w.Z
+  // The mixed path runs the first sweeps with the B Z product on the tensor cores (complex64
+  // operands, FP32-accurate BF16x9 products) down to the FP32 level, then finishes in complex128.
+  const bool mixed = h->prec == CX_PREC_MIXED;
   auto refine = [&](bool* conv) -> cx_status {
     *conv = false;
     k_split_diag<<<gn, 256, 0, st>>>(w.B, w.ev, w.Z, n);
     h->launches++;
+    bool fp32 = mixed;
+    if (fp32) {
+      k_d2f<<<gn, 256, 0, st>>>(w.B, w.Gf, n2);
+      h->launches++;
+    }
     double prev = 1e300;
     for (int it = 0; it < 80; ++it) {
-      CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, (const cuDoubleComplex*)w.B, n,
-                                 (const cuDoubleComplex*)w.Z, n, &zero, (cuDoubleComplex*)w.EZ, n));
       CX_TRY_CUDA(h, cudaMemsetAsync(w.dmax, 0, 8, st));
-      k_sylv_update<<<gn, 256, 0, st>>>(w.B, w.EZ, w.ev, w.Z, w.Zn, n, (unsigned long long*)w.dmax);
-      h->launches++;
+      if (fp32) {
+        const cuComplex c1 = make_cuComplex(1, 0), c0 = make_cuComplex(0, 0);
+        k_d2f<<<gn, 256, 0, st>>>(w.Z, w.Mf, n2);
+        CX_TRY_BLAS(h, cublasSetMathMode(h->cublas, CUBLAS_FP32_EMULATED_BF16X9_MATH));
+        CX_TRY_BLAS(h, cublasCgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &c1, (const cuComplex*)w.Gf, n,
+                                   (const cuComplex*)w.Mf, n, &c0, (cuComplex*)w.Cf, n));
+        CX_TRY_BLAS(h, cublasSetMathMode(h->cublas, CUBLAS_DEFAULT_MATH));
+        k_sylv_update<float2><<<gn, 256, 0, st>>>(w.B, w.Cf, w.ev, w.Z, w.Zn, n, (unsigned long long*)w.dmax);
+        h->launches += 2;
+      } else {
+        CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, (const cuDoubleComplex*)w.B, n,
+                                   (const cuDoubleComplex*)w.Z, n, &zero, (cuDoubleComplex*)w.EZ, n));
+        k_sylv_update<double2><<<gn, 256, 0, st>>>(w.B, w.EZ, w.ev, w.Z, w.Zn, n, (unsigned long long*)w.dmax);
+        h->launches++;
+      }
       std::swap(w.Z, w.Zn);
       double dm = 0;
       CX_TRY_CUDA(h, cudaMemcpyAsync(&dm, w.dmax, 8, cudaMemcpyDeviceToHost, st));
       CX_TRY_CUDA(h, cudaStreamSynchronize(st));
       if (!(dm < 1e300)) return CX_OK;                       // diverged (inf / NaN)
-      if (dm < 1e-12) { *conv = true; break; }
+      if (fp32) {
+        // FP32 level reached (or the complex64 sweeps stall): continue in complex128
+        if (dm < 1e-6 || (it >= 8 && dm > 0.9 * prev)) { fp32 = false; prev = 1e300; }
+        else prev = dm;
+        continue;
+      }
+      if (dm < (mixed ? 1e-10 : 1e-12)) { *conv = true; break; }
       if (it >= 8 && dm > 0.9 * prev) return CX_OK;          // not contracting
       prev = dm;
     }

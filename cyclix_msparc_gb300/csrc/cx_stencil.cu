@@ -271,74 +271,62 @@ nl_contract_kernel(const int N, const BlockDev<R>* __restrict__ blocks, const in
 // Kleinman-Bylander apply as its own pass (used after the TMA stencil, which leaves it out):
 //   out[p, s] += alpha_b * sum_{entries e of p} Chi_e . Cp[s][seg_e][:]
 // (the scatter of src/h_nonlocal_vector_mult.m:38-42, scaled like the rest of the Chebyshev step).
-// A CTA owns one 32-point row chunk (a radial tile row that some projector ball touches) and
-// 8 warps x NSW states: each warp reads a point's entries once (16-byte loads) and accumulates them
-// into NSW states at a time, so the dependent coefficient loads of the states overlap.
-constexpr int NSW = 4;   // states per warp in nl_apply_kernel
-
-template <typename R>
-__device__ __forceinline__ void load_chi4(const R* p, R c[4]) {
-  if constexpr (sizeof(R) == 4) {
-    const float4 v = *reinterpret_cast<const float4*>(p);
-    c[0] = v.x; c[1] = v.y; c[2] = v.z; c[3] = v.w;
-  } else {
-    const double2 a = *reinterpret_cast<const double2*>(p), b = *reinterpret_cast<const double2*>(p + 2);
-    c[0] = a.x; c[1] = a.y; c[2] = b.x; c[3] = b.y;
-  }
-}
-template <typename R>
-__device__ __forceinline__ void load_cp4(const cplx<R>* p, cplx<R> c[4]) {
-  if constexpr (sizeof(R) == 4) {
-    const float4 a = *reinterpret_cast<const float4*>(p), b = *reinterpret_cast<const float4*>(p + 2);
-    c[0] = make_float2(a.x, a.y); c[1] = make_float2(a.z, a.w); c[2] = make_float2(b.x, b.y); c[3] = make_float2(b.z, b.w);
-  } else {
-#pragma unroll
-    for (int q = 0; q < 4; ++q) c[q] = p[q];
-  }
-}
+// Per 32-point row chunk that projector balls touch, the entries form a small dense matrix
+// Chi_c (32 points x K = 4 x segments of the chunk, zero where a point is outside a ball), so the
+// apply is Y[chunk, states] += Chi_c . Cp_c[K, states]: a CTA owns one chunk and 32 states, stages
+// Cp_c of its states in shared memory, and each warp accumulates 4 states for its 32 points with
+// coalesced Chi_c loads and broadcast shared-memory reads.
+constexpr int NA_SPW = 4;      // states per warp
+constexpr int NA_SPC = 8 * NA_SPW;
 
 template <typename R>
 __global__ void __launch_bounds__(256)
 nl_apply_kernel(const int N, const int Nx, const BlockDev<R>* __restrict__ blocks, const StepScalars* __restrict__ scal,
-                const int2* __restrict__ state_tab, const int nstates, const int out_sel, const int* __restrict__ chunks,
-                const int32_t* __restrict__ ent_start, const int32_t* __restrict__ ent_count, const int32_t* __restrict__ ent_seg,
-                const R* __restrict__ ent_chi, const cplx<R>* __restrict__ cprime, const int nseg) {
+                const int2* __restrict__ state_tab, const int nstates, const int out_sel, const ChunkTables ct,
+                const cplx<R>* __restrict__ cprime, const int nseg) {
+  extern __shared__ __align__(16) unsigned char nl_smem[];
+  cplx<R>* cs = (cplx<R>*)nl_smem;                       // [NA_SPC][K]
+  const int c = blockIdx.x;
+  const int p0 = ct.p0[c];
+  const int sb = ct.seg_ptr[c], nsc = ct.seg_ptr[c + 1] - sb;
+  const int K = nsc * kAngMax;
+  const int gsb = blockIdx.y * NA_SPC;
+  const int nst_cta = min(NA_SPC, nstates - gsb);
+  for (int i = threadIdx.x; i < nst_cta * K; i += blockDim.x) {
+    const int sl = i / K, k = i - sl * K;
+    const int sg = ct.segs[sb + k / kAngMax];
+    cs[i] = cprime[((size_t)(gsb + sl) * nseg + sg) * kAngMax + (k % kAngMax)];
+  }
+  __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int gs0 = (blockIdx.y * 8 + w) * NSW;
-  if (gs0 >= nstates) return;
-  const int p0 = chunks[blockIdx.x];
+  const int sl0 = w * NA_SPW;
+  if (sl0 >= nst_cta) return;
+  const int nst = min(NA_SPW, nst_cta - sl0);
   const int r = p0 % Nx + lane;
-  if (r >= Nx) return;
-  const int p = p0 + lane;
-  const int e0 = ent_start[p], ne = ent_count[p];
-  if (ne == 0) return;
-  const int nst = min(NSW, nstates - gs0);
-  cplx<R> acc[NSW];
+  const bool ok = r < Nx;
+  const R* __restrict__ chi = (const R*)ct.chi + ct.chi_ptr[c] + lane;     // [K][32]
+  cplx<R> acc[NA_SPW];
 #pragma unroll
-  for (int k = 0; k < NSW; ++k) acc[k] = mk<R>((R)0, (R)0);
-  for (int e = e0; e < e0 + ne; ++e) {
-    const int sg = ent_seg[e];
-    R ch[4];
-    load_chi4<R>(ent_chi + (size_t)e * kAngMax, ch);
+  for (int j = 0; j < NA_SPW; ++j) acc[j] = mk<R>((R)0, (R)0);
+  for (int k = 0; k < K; ++k) {
+    const R x = chi[(size_t)k * 32];
 #pragma unroll
-    for (int k = 0; k < NSW; ++k) {
-      if (k < nst) {
-        cplx<R> cs[4];
-        load_cp4<R>(cprime + ((size_t)(gs0 + k) * nseg + sg) * kAngMax, cs);
-#pragma unroll
-        for (int q = 0; q < kAngMax; ++q) cfma(acc[k], ch[q], cs[q]);
-      }
+    for (int j = 0; j < NA_SPW; ++j) {
+      const cplx<R> v = cs[(sl0 + j) * K + k];
+      acc[j].x = fma(x, v.x, acc[j].x);
+      acc[j].y = fma(x, v.y, acc[j].y);
     }
   }
+  if (!ok) return;
 #pragma unroll
-  for (int k = 0; k < NSW; ++k) {
-    if (k < nst) {
-      const int2 bs = state_tab[gs0 + k];
+  for (int j = 0; j < NA_SPW; ++j) {
+    if (j < nst) {
+      const int2 bs = state_tab[gsb + sl0 + j];
       const R alpha = (R)scal[bs.x].alpha;
-      cplx<R>* out = blocks[bs.x].buf[out_sel] + (size_t)bs.y * N + p;
+      cplx<R>* out = blocks[bs.x].buf[out_sel] + (size_t)bs.y * N + p0 + lane;
       cplx<R> o = *out;
-      o.x = fma(alpha, acc[k].x, o.x);
-      o.y = fma(alpha, acc[k].y, o.y);
+      o.x = fma(alpha, acc[j].x, o.x);
+      o.y = fma(alpha, acc[j].y, o.y);
       *out = o;
     }
   }
@@ -346,21 +334,24 @@ nl_apply_kernel(const int N, const int Nx, const BlockDev<R>* __restrict__ block
 
 template <typename R>
 cudaError_t launch_nl_apply(const GridDev& g, const BlockDev<R>* blocks, const StepScalars* scal, const int2* state_tab, int nstates,
-                            int out_sel, const int* chunks, int nchunks, const int32_t* ent_start, const int32_t* ent_count,
-                            const NonlocalDev& nl, const cplx<R>* cprime, cudaStream_t st) {
-  if (nchunks == 0 || nl.nseg == 0) return cudaSuccess;
-  dim3 grid((unsigned)nchunks, (unsigned)((nstates + 8 * NSW - 1) / (8 * NSW)));
+                            int out_sel, const ChunkTables& ct, const cplx<R>* cprime, int nseg, cudaStream_t st) {
+  if (ct.nchunks == 0 || nseg == 0) return cudaSuccess;
+  dim3 grid((unsigned)ct.nchunks, (unsigned)((nstates + NA_SPC - 1) / NA_SPC));
   if (grid.y > 65535) return cudaErrorInvalidConfiguration;
-  nl_apply_kernel<R><<<grid, 256, 0, st>>>(g.N, g.Nx, blocks, scal, state_tab, nstates, out_sel, chunks, ent_start, ent_count, nl.ent_seg,
-                                           (const R*)nl.ent_chi, cprime, nl.nseg);
+  const size_t smem = (size_t)NA_SPC * ct.kmax * sizeof(cplx<R>);
+  if (smem > 48 * 1024) {
+    if (smem > 200 * 1024) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(nl_apply_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  nl_apply_kernel<R><<<grid, 256, smem, st>>>(g.N, g.Nx, blocks, scal, state_tab, nstates, out_sel, ct, cprime, nseg);
   return cudaGetLastError();
 }
 
-template cudaError_t launch_nl_apply<float>(const GridDev&, const BlockDev<float>*, const StepScalars*, const int2*, int, int, const int*,
-                                            int, const int32_t*, const int32_t*, const NonlocalDev&, const cplx<float>*, cudaStream_t);
+template cudaError_t launch_nl_apply<float>(const GridDev&, const BlockDev<float>*, const StepScalars*, const int2*, int, int,
+                                            const ChunkTables&, const cplx<float>*, int, cudaStream_t);
 template cudaError_t launch_nl_apply<double>(const GridDev&, const BlockDev<double>*, const StepScalars*, const int2*, int, int,
-                                             const int*, int, const int32_t*, const int32_t*, const NonlocalDev&, const cplx<double>*,
-                                             cudaStream_t);
+                                             const ChunkTables&, const cplx<double>*, int, cudaStream_t);
 
 template <typename R, int F, bool HEL>
 static cudaError_t launch_one(const StepArgs<R>& a, dim3 grid, cudaStream_t st) {
