@@ -209,62 +209,86 @@ cheb_step_kernel(const StepArgs<R> A) {
 // Contraction of the KB projectors with the block: for atom J and state s,
 //   C[J,q,s] = gamma_Jq * sum_img exp(i k.(R_J - R_img)) * sum_n (W Chi_img)[n,q] * in[pos_n, s]
 // and the per-image scatter coefficients Cp[s][img][q] = exp(-i k.(R_J - R_img)) C[J,q,s]
-// (src/h_nonlocal_vector_mult.m:30-43).  One CTA per (atom, state); no atomics.
+// (src/h_nonlocal_vector_mult.m:30-43).  One CTA per (atom, NC_SPC states): the threads walk the
+// atom's ball nodes (consecutive along r, so each state's loads coalesce) and read a node's data
+// (position, segment, W Chi) once for the NC_SPC states; no atomics.
+constexpr int NC_SPC = 4;
 template <typename R>
 __global__ void __launch_bounds__(128)
-nl_contract_kernel(const int N, const BlockDev<R>* __restrict__ blocks, const int2* __restrict__ state_tab, const int in_sel,
-                   const NonlocalDev nl, const R* __restrict__ node_wchi, cplx<R>* __restrict__ cprime) {
+nl_contract_kernel(const int N, const int nstates, const BlockDev<R>* __restrict__ blocks, const int2* __restrict__ state_tab,
+                   const int in_sel, const NonlocalDev nl, const R* __restrict__ node_wchi, cplx<R>* __restrict__ cprime) {
   const int J = blockIdx.x;
-  const int gs = blockIdx.y;
-  const int2 bs = state_tab[gs];
-  const cplx<R>* __restrict__ y = blocks[bs.x].buf[in_sel] + (size_t)bs.y * N;
-  const double2* __restrict__ ph = nl.seg_phase + (size_t)bs.x * nl.nseg;
+  const int gs0 = blockIdx.y * NC_SPC;
+  const int nst = min(NC_SPC, nstates - gs0);
+  const cplx<R>* y[NC_SPC];
+  const double2* ph[NC_SPC];
+#pragma unroll
+  for (int j = 0; j < NC_SPC; ++j) {
+    const int2 bs = state_tab[gs0 + (j < nst ? j : 0)];
+    y[j] = blocks[bs.x].buf[in_sel] + (size_t)bs.y * N;
+    ph[j] = nl.seg_phase + (size_t)bs.x * nl.nseg;
+  }
   const int n0 = nl.atom_node_ptr[J], n1 = nl.atom_node_ptr[J + 1];
-  R ax[kAngMax], ay[kAngMax];
+  R a[NC_SPC][2 * kAngMax];
 #pragma unroll
-  for (int q = 0; q < kAngMax; ++q) { ax[q] = 0; ay[q] = 0; }
+  for (int j = 0; j < NC_SPC; ++j)
+#pragma unroll
+    for (int q = 0; q < 2 * kAngMax; ++q) a[j][q] = 0;
+#pragma unroll 2
   for (int n = n0 + threadIdx.x; n < n1; n += blockDim.x) {
-    const cplx<R> v = y[nl.node_pos[n]];
-    const double2 p = ph[nl.node_seg[n]];
-    const R vx = v.x * (R)p.x - v.y * (R)p.y;
-    const R vy = v.x * (R)p.y + v.y * (R)p.x;
+    const int pos = nl.node_pos[n];
+    const int sg = nl.node_seg[n];
+    R wq[kAngMax];
 #pragma unroll
-    for (int q = 0; q < kAngMax; ++q) {
-      const R w = node_wchi[(size_t)n * kAngMax + q];
-      ax[q] = fma(w, vx, ax[q]);
-      ay[q] = fma(w, vy, ay[q]);
+    for (int q = 0; q < kAngMax; ++q) wq[q] = node_wchi[(size_t)n * kAngMax + q];
+#pragma unroll
+    for (int j = 0; j < NC_SPC; ++j) {
+      if (j < nst) {
+        const cplx<R> v = y[j][pos];
+        const double2 p = ph[j][sg];
+        const R vx = v.x * (R)p.x - v.y * (R)p.y;
+        const R vy = v.x * (R)p.y + v.y * (R)p.x;
+#pragma unroll
+        for (int q = 0; q < kAngMax; ++q) {
+          a[j][2 * q] = fma(wq[q], vx, a[j][2 * q]);
+          a[j][2 * q + 1] = fma(wq[q], vy, a[j][2 * q + 1]);
+        }
+      }
     }
   }
-  __shared__ R red[2 * kAngMax][32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  // CTA reduction: warps by shuffles, then across warps in shared memory
+  constexpr int NV = NC_SPC * 2 * kAngMax;
+  __shared__ R red[4][NV];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
-  for (int q = 0; q < kAngMax; ++q) {
+  for (int j = 0; j < NC_SPC; ++j)
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      ax[q] += __shfl_xor_sync(0xffffffffu, ax[q], o);
-      ay[q] += __shfl_xor_sync(0xffffffffu, ay[q], o);
+    for (int q = 0; q < 2 * kAngMax; ++q) {
+      R v = a[j][q];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) red[w][j * 2 * kAngMax + q] = v;
     }
-  }
-  if (lane == 0) {
-#pragma unroll
-    for (int q = 0; q < kAngMax; ++q) { red[2 * q][wid] = ax[q]; red[2 * q + 1][wid] = ay[q]; }
-  }
   __syncthreads();
-  const int nw = blockDim.x >> 5;
+  // threads (state j, segment, q) write the scaled, re-phased coefficients: conj(p) gamma C
   const int s0 = nl.atom_seg_ptr[J], s1 = nl.atom_seg_ptr[J + 1];
-  // threads (seg, q) write the scaled, re-phased coefficients
-  for (int w = threadIdx.x; w < (s1 - s0) * kAngMax; w += blockDim.x) {
-    const int q = w % kAngMax, sg = s0 + w / kAngMax;
+  const int nout = nst * (s1 - s0) * kAngMax;
+  const int nw = blockDim.x >> 5;
+  for (int o = threadIdx.x; o < nout; o += blockDim.x) {
+    const int q = o % kAngMax, sg = s0 + (o / kAngMax) % (s1 - s0), j = o / (kAngMax * (s1 - s0));
     R sx = 0, sy = 0;
-    for (int k = 0; k < nw; ++k) { sx += red[2 * q][k]; sy += red[2 * q + 1][k]; }
+    for (int k = 0; k < nw; ++k) {
+      sx += red[k][j * 2 * kAngMax + 2 * q];
+      sy += red[k][j * 2 * kAngMax + 2 * q + 1];
+    }
     const R gmm = (R)nl.gamma[(size_t)J * kAngMax + q];
-    sx *= gmm; sy *= gmm;
-    const double2 p = ph[sg];
-    // conj(p) * (sx + i sy)
-    cplx<R> o;
-    o.x = sx * (R)p.x + sy * (R)p.y;
-    o.y = sy * (R)p.x - sx * (R)p.y;
-    cprime[((size_t)gs * nl.nseg + sg) * kAngMax + q] = o;
+    sx *= gmm;
+    sy *= gmm;
+    const double2 p = nl.seg_phase[(size_t)state_tab[gs0 + j].x * nl.nseg + sg];
+    cplx<R> out;
+    out.x = sx * (R)p.x + sy * (R)p.y;
+    out.y = sy * (R)p.x - sx * (R)p.y;
+    cprime[((size_t)(gs0 + j) * nl.nseg + sg) * kAngMax + q] = out;
   }
 }
 
@@ -418,8 +442,8 @@ cudaError_t launch_nl_contract(const GridDev& g, const BlockDev<R>* blocks, cons
                                int in_sel, const NonlocalDev& nl, cplx<R>* cprime, cudaStream_t st) {
   if (nl.n_atm == 0 || nl.nseg == 0) return cudaSuccess;
   if (nstates > 65535) return cudaErrorInvalidConfiguration;
-  dim3 grid((unsigned)nl.n_atm, (unsigned)nstates);
-  nl_contract_kernel<R><<<grid, 128, 0, st>>>(g.N, blocks, state_tab, in_sel, nl, (const R*)nl.node_wchi, cprime);
+  dim3 grid((unsigned)nl.n_atm, (unsigned)((nstates + NC_SPC - 1) / NC_SPC));
+  nl_contract_kernel<R><<<grid, 128, 0, st>>>(g.N, nstates, blocks, state_tab, in_sel, nl, (const R*)nl.node_wchi, cprime);
   return cudaGetLastError();
 }
 

@@ -14,6 +14,8 @@
  *                         src/eigSolver.m:1, called from src/scf.m:123-124
  *   cx_poisson          S = poissonSolve(S,poisson_tol,Isguess) -> aar(Lap_std,f,...)
  *                         src/poissonSolve.m:1, src/aar.m:1
+ *   cx_scf              S = scf(S): the SCF loop around eigSolver (first relaxation step,
+ *                         nspin = 1, potential mixing) src/scf.m:1-327
  *
  * The operator data that MATLAB keeps in the struct S (grid, FD weights,
  * quadrature weights, KB projector images) is handed over once in cx_create;
