@@ -80,9 +80,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// bounded wait: true when the phase completed, false after the iteration limit
+// bounded wait: true when the phase completed, false after about a second (2^31 SM cycles)
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  for (int i = 0; i < (1 << 22); ++i)
+  if (mbar_try_wait(bar, parity)) return true;
+  const long long t_end = clock64() + (1LL << 31);
+  while (clock64() < t_end)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }

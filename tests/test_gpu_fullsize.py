@@ -1,0 +1,96 @@
+"""GPU checks at the full sizes of the batched, helical and full-SCF workloads.
+
+The oracle cannot run these sizes in seconds, so the checks are size-independent properties:
+  * the complex64 kernels (TMA stencil with one or several theta tiles, the helical variant with
+    three theta rows per thread, projector contraction and apply) agree with the complex128
+    kernels on seeded blocks: max |Y32 - Y64| / max |Y64| <= 2e-6 for H*psi and <= 1e-5 for a
+    degree-6 Chebyshev filter (the complex128 path is the one pinned to the oracle at small sizes);
+  * linearity of H*psi: H(a x + b y) = a H x + b H y to 1e-12 relative (complex128);
+  * the batched eigensolver (16 Bloch blocks of uneven Ns) gives the same lowest eigenvalues in
+    mixed precision as in FP64 after two steps from a random start: <= 1e-3 Ha on the lowest half
+    of each block (the two trajectories are not converged yet; converged results are compared
+    through the SCF energy).
+Blocks keep the workloads' Bloch points and spins; the H*psi checks use a few states per block.
+"""
+import numpy as np
+import pytest
+
+from cyclix_msparc_gb300.workloads import WORKLOADS, block_layout, initial_psi, make_system
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "cyclic-batched-16nu-64x16x48-ns96to320-m24": "one theta tile of 16 rows, 16 nu blocks",
+    "helical-80x32x40-96k2s-ns192-m24": "helical, 32 theta rows in one tile (3 rows per thread), eta / nu / spin blocks",
+    "scf-128x48x96-384at-8k-ns1024": "two theta tiles of 24 rows with TMA halos, 384 atoms",
+}
+
+
+def _rand(N, n, seed):
+    rng = np.random.default_rng(seed)
+    return np.asfortranarray(rng.standard_normal((N, n)) + 1j * rng.standard_normal((N, n)))
+
+
+@pytest.fixture(scope="module", params=list(CASES))
+def fullsize(request):
+    wl = WORKLOADS[request.param]
+    S = make_system(wl)
+    if S.Veff is None:
+        # the SCF workload carries no potential: use the initial electrostatics-like field
+        S.Veff = np.repeat((-S.rho_at)[:, None], S.nspin, axis=1)
+    bl = block_layout(wl, S)
+    pick = sorted({0, len(bl) // 2, len(bl) - 1})
+    blocks = [(bl[i][0], bl[i][1], 4) for i in pick]
+    return wl, S, blocks
+
+
+def test_fullsize_mixed_matches_fp64(fullsize):
+    from cyclix_msparc_gb300.msparc import CyclixGPU
+    wl, S, blocks = fullsize
+    g64 = CyclixGPU(S, blocks, "fp64")
+    g32 = CyclixGPU(S, blocks, "mixed")
+    try:
+        for b in range(len(blocks)):
+            X = _rand(S.N, 3, 100 + b)
+            Y64 = g64.hpsi(b, X)
+            Y32 = g32.hpsi(b, X)
+            assert np.max(np.abs(Y32 - Y64)) <= 2e-6 * np.max(np.abs(Y64)), (wl.name, b)
+            F64 = g64.filter(b, X, 6, 10.0, 3000.0, -5.0)
+            F32 = g32.filter(b, X, 6, 10.0, 3000.0, -5.0)
+            assert np.max(np.abs(F32 - F64)) <= 1e-5 * np.max(np.abs(F64)), (wl.name, b)
+        # linearity (complex128)
+        x, y = _rand(S.N, 1, 7), _rand(S.N, 1, 8)
+        a, c = 0.3 - 1.1j, 2.0 + 0.5j
+        lhs = g64.hpsi(0, a * x + c * y)
+        rhs = a * g64.hpsi(0, x) + c * g64.hpsi(0, y)
+        assert np.max(np.abs(lhs - rhs)) <= 1e-12 * np.max(np.abs(rhs))
+    finally:
+        g64.close()
+        g32.close()
+
+
+def test_fullsize_batched_eigensolver_mixed_vs_fp64():
+    from cyclix_msparc_gb300.msparc import CyclixGPU
+    wl = WORKLOADS["cyclic-batched-16nu-64x16x48-ns96to320-m24"]
+    S = make_system(wl)
+    bl = block_layout(wl, S)
+    nblk = len(bl)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        g = CyclixGPU(S, bl, prec)
+        try:
+            for b, (_, _, n) in enumerate(bl):
+                g.set_psi(b, initial_psi(S.N, n, 500 + b))
+            EV = np.zeros(sum(n for (_, _, n) in bl))
+            a0, bup, lc = np.zeros(nblk), np.zeros(nblk), np.zeros(nblk)
+            for count in (1, 2):
+                g.eigsolve(count, wl.npl, EV, a0, bup, lc)
+            out[prec] = EV.copy()
+        finally:
+            g.close()
+    off = 0
+    for (_, _, n) in bl:
+        lo = n // 2
+        err = np.max(np.abs(out["mixed"][off:off + lo] - out["fp64"][off:off + lo]))
+        assert err <= 1e-3, (n, err)
+        off += n
