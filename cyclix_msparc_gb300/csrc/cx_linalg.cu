@@ -488,13 +488,14 @@ cx_status rr_rotate<float>(cx_handle h, const float2* X, float2* out, int N, int
   return CX_OK;
 }
 
-// Eigen-decomposition of the projected Hs (n x n, complex128, general) into w.ev / w.V.
-// Fast path: with Gwq = Q^H W Q = L L^H, T = L^H Hs L^-H is Hermitian up to the subspace residual
-// (the Hamiltonian is self-adjoint in the W inner product); the Hermitian eigenvectors U of
-// (T + T^H)/2 make B = U^H T U nearly diagonal, and the fixed point B X = X Lambda with X = I + Z is
-// iterated to convergence, giving the eigenpairs of Hs exactly (Y = L^-H U X).  When the iteration
-// does not converge (clustered spectrum, first steps) the general solver cusolverDnXgeev is used.
-// Returns in *used_fallback whether geev ran.
+// Eigenpairs of the Ritz pencil A = G^-1 M (w.Hs, n x n complex128, not Hermitian for Cyclix
+// cells) into w.ev and the rotation coefficients c into w.V.  With the W-Gram Gw = X^H W X =
+// U_w^H U_w, T = U_w A U_w^-1 is similar to A and Hermitian up to the subspace residual (the
+// Hamiltonian is self-adjoint in the W inner product).  Tier 1 iterates the fixed point
+// T X = X Lambda with X = I + Z directly; tier 2 starts it from the Hermitian eigenvectors U of
+// (T + T^H)/2 (B = U^H T U); c = U_w^-1 (U) X.  When neither converges (clustered spectrum, first
+// steps) the general solver cusolverDnXgeev runs on Hs = R A R^-1 (R = chol(G) in w.G) and
+// c = R^-1 v.  Returns in *used_fallback whether geev ran.
 static cx_status subspace_eig(cx_handle h, int n, RRWork& w, bool* used_fallback) {
   const cuDoubleComplex one = make_cuDoubleComplex(1, 0), zero = make_cuDoubleComplex(0, 0);
   const size_t n2 = (size_t)n * n;
@@ -503,9 +504,9 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, bool* used_fallback
   *used_fallback = false;
   CX_TRY_BLAS(h, cublasSetMathMode(h->cublas, CUBLAS_DEFAULT_MATH));
   CX_TRY_CUDA(h, cudaMemcpyAsync(w.Hs0, w.Hs, n2 * 16, cudaMemcpyDeviceToDevice, st));
-  // L = chol(Gwq) (lower)
+  // U_w = chol(Gw) (upper)
   size_t wsd = 0, wsh = 0;
-  CX_TRY_SOLVER(h, cusolverDnXpotrf_bufferSize(h->cusolver, h->cusolver_params, CUBLAS_FILL_MODE_LOWER, n, CUDA_C_64F, w.Gw, n,
+  CX_TRY_SOLVER(h, cusolverDnXpotrf_bufferSize(h->cusolver, h->cusolver_params, CUBLAS_FILL_MODE_UPPER, n, CUDA_C_64F, w.Gw, n,
                                                 CUDA_C_64F, &wsd, &wsh));
   size_t wsd2 = 0, wsh2 = 0;
   CX_TRY_SOLVER(h, cusolverDnXsyevd_bufferSize(h->cusolver, h->cusolver_params, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n,
@@ -521,7 +522,7 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, bool* used_fallback
     CX_TRY_CUDA(h, cudaMallocHost(&h->h_ws, wsh + 256));
     h->hws_bytes = wsh + 256;
   }
-  CX_TRY_SOLVER(h, cusolverDnXpotrf(h->cusolver, h->cusolver_params, CUBLAS_FILL_MODE_LOWER, n, CUDA_C_64F, w.Gw, n, CUDA_C_64F,
+  CX_TRY_SOLVER(h, cusolverDnXpotrf(h->cusolver, h->cusolver_params, CUBLAS_FILL_MODE_UPPER, n, CUDA_C_64F, w.Gw, n, CUDA_C_64F,
                                      h->d_ws, h->ws_bytes, h->h_ws, h->hws_bytes, w.info));
   int info = 0;
   CX_TRY_CUDA(h, cudaMemcpyAsync(&info, w.info, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -583,11 +584,11 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, bool* used_fallback
     return CX_OK;
   };
   if (fast) {
-    // T = L^H (Hs L^-H)
-    CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT, n, n, &one,
-                               (const cuDoubleComplex*)w.Gw, n, (cuDoubleComplex*)w.Hs, n));
-    CX_TRY_BLAS(h, cublasZtrmm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT, n, n, &one,
+    // T = (U_w A) U_w^-1
+    CX_TRY_BLAS(h, cublasZtrmm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
                                (const cuDoubleComplex*)w.Gw, n, (const cuDoubleComplex*)w.Hs, n, (cuDoubleComplex*)w.T, n));
+    CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
+                               (const cuDoubleComplex*)w.Gw, n, (cuDoubleComplex*)w.T, n));
     // tier 1: the filtered block is ordered like the previous Ritz vectors, so near self-consistency T
     // itself is nearly diagonal -- refine directly (U = I)
     CX_TRY_CUDA(h, cudaMemcpyAsync(w.B, w.T, n2 * 16, cudaMemcpyDeviceToDevice, st));
@@ -595,9 +596,9 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, bool* used_fallback
     cx_status rs = refine(&conv);
     if (rs != CX_OK) return rs;
     if (conv) {
-      // eigenvectors of Hs: Y = L^-H X
+      // eigenvectors of A: c = U_w^-1 X
       CX_TRY_CUDA(h, cudaMemcpyAsync(w.V, w.Z, n2 * 16, cudaMemcpyDeviceToDevice, st));
-      CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT, n, n, &one,
+      CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
                                  (const cuDoubleComplex*)w.Gw, n, (cuDoubleComplex*)w.V, n));
       return CX_OK;
     }
@@ -615,18 +616,21 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, bool* used_fallback
     if (info == 0) {
       if ((rs = refine(&conv)) != CX_OK) return rs;
       if (conv) {
-        // eigenvectors of Hs: Y = L^-H (U X)
+        // eigenvectors of A: c = U_w^-1 (U X)
         CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, (const cuDoubleComplex*)w.U, n,
                                    (const cuDoubleComplex*)w.Z, n, &zero, (cuDoubleComplex*)w.V, n));
-        CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT, n, n, &one,
+        CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
                                    (const cuDoubleComplex*)w.Gw, n, (cuDoubleComplex*)w.V, n));
         return CX_OK;
       }
     }
   }
-  // general FP64 eigensolver on the untouched Hs
+  // general FP64 eigensolver on Hs = R A R^-1 (the reference's matrix, better conditioned than A)
   *used_fallback = true;
-  CX_TRY_CUDA(h, cudaMemcpyAsync(w.Hs, w.Hs0, n2 * 16, cudaMemcpyDeviceToDevice, st));
+  CX_TRY_BLAS(h, cublasZtrmm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
+                             (const cuDoubleComplex*)w.G, n, (const cuDoubleComplex*)w.Hs0, n, (cuDoubleComplex*)w.Hs, n));
+  CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
+                             (const cuDoubleComplex*)w.G, n, (cuDoubleComplex*)w.Hs, n));
   size_t g1 = 0, g2 = 0;
   CX_TRY_SOLVER(h, cusolverDnXgeev_bufferSize(h->cusolver, h->cusolver_params, CUSOLVER_EIG_MODE_NOVECTOR, CUSOLVER_EIG_MODE_VECTOR, n,
                                                CUDA_C_64F, w.Hs, n, CUDA_C_64F, w.ev, CUDA_C_64F, nullptr, n, CUDA_C_64F, w.V, n,
@@ -648,6 +652,9 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, bool* used_fallback
     h->err = "eigensolver: geev failed (info " + std::to_string(info) + ")";
     return CX_ERR_LIB;
   }
+  // rotation coefficients c = R^-1 v
+  CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
+                             (const cuDoubleComplex*)w.G, n, (cuDoubleComplex*)w.V, n));
   return CX_OK;
 }
 
@@ -686,15 +693,13 @@ static cx_status rayleigh_ritz_block(cx_handle h, int b, int sel, RRWork& w, dou
   }
   const cuDoubleComplex one = make_cuDoubleComplex(1, 0);
   CX_TRY_BLAS(h, cublasSetMathMode(h->cublas, CUBLAS_DEFAULT_MATH));
-  // Hs = R^-H M R^-1 and Gwq = R^-H Gw R^-1 (orthonormal basis Q = X R^-1 of the same span as orth(X))
+  // A = G^-1 M = R^-1 R^-H M: the Ritz pencil M c = lambda G c.  The reference's projected matrix
+  // in the orthonormal basis Q = X R^-1 (the span of orth(X)) is Hs = R A R^-1, with the same
+  // eigenvalues; its eigenvectors map to the rotation coefficients c = R^-1 v.
   CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT, n, n, &one,
                              (const cuDoubleComplex*)w.G, n, (cuDoubleComplex*)w.Hs, n));
-  CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
+  CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
                              (const cuDoubleComplex*)w.G, n, (cuDoubleComplex*)w.Hs, n));
-  CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_C, CUBLAS_DIAG_NON_UNIT, n, n, &one,
-                             (const cuDoubleComplex*)w.G, n, (cuDoubleComplex*)w.Gw, n));
-  CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
-                             (const cuDoubleComplex*)w.G, n, (cuDoubleComplex*)w.Gw, n));
   // eigenpairs of Hs (general; eigSolver.m:110 -- Hs is not Hermitian for Cyclix cells)
   bool fb = false;
   if ((s = subspace_eig(h, n, w, &fb)) != CX_OK) return s;
@@ -710,10 +715,8 @@ static cx_status rayleigh_ritz_block(cx_handle h, int b, int sel, RRWork& w, dou
   CX_TRY_CUDA(h, cudaMemcpyAsync(w.perm, perm.data(), n * sizeof(int), cudaMemcpyHostToDevice, h->stream));
   k_gather_cols<<<grid_for((size_t)n * n), 256, 0, h->stream>>>(w.V, w.Hs, n, w.perm);
   h->launches++;
-  // C = R^-1 Q  (into w.V)
+  // rotation coefficients C (sorted eigenvectors of the pencil, into w.V)
   CX_TRY_CUDA(h, cudaMemcpyAsync(w.V, w.Hs, (size_t)n * n * 16, cudaMemcpyDeviceToDevice, h->stream));
-  CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
-                             (const cuDoubleComplex*)w.G, n, (cuDoubleComplex*)w.V, n));
   // psi = X C  (into the other buffer), then W-normalise (eigSolver.m:119-124)
   if ((s = rr_rotate<R>(h, X, HX, N, n, w)) != CX_OK) return s;
   k_colnorm_w<R><<<n, 256, 0, h->stream>>>(HX, h->d_W, N, w.scfac);
