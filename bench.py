@@ -243,6 +243,82 @@ def e2e_host(g, count, npl, steps, bounds):
     return dt * 1e3, nbytes, nbytes
 
 
+# ----------------------------------------------------------------------------- all configurations
+CONFIGS = [
+    ("cyclic-40x12x20-ns48-m20", True),
+    ("cyclic-96x24x64-ns256-m24", True),
+    ("cyclic-batched-16nu-64x16x48-ns96to320-m24", True),
+    ("helical-80x32x40-96k2s-ns192-m24", True),
+    ("scf-128x48x96-384at-8k-ns1024", False),   # FP64 Rayleigh-Ritz of 8 x ~1000 states: minutes per step
+]
+
+
+def config_lines():
+    """One eigSolver step per configuration (mixed and, where it fits the run, FP64), plus the full
+    mixed-precision SCF of the 384-atom cell.  One JSON line per configuration on stdout."""
+    from cyclix_msparc_gb300.msparc import CyclixGPU
+    from cyclix_msparc_gb300.workloads import WORKLOADS, block_layout, initial_psi, make_system
+    for name, with_fp64 in CONFIGS:
+        wl = WORKLOADS[name]
+        t0 = time.perf_counter()
+        S = make_system(wl)
+        setup_s = time.perf_counter() - t0
+        scf_cell = S.Veff is None
+        if scf_cell:
+            S.Veff = np.repeat((-S.rho_at)[:, None], S.nspin, axis=1)
+        blocks = block_layout(wl, S)
+        nblk = len(blocks)
+        res = {"workload": name, "N": S.N, "blocks": nblk, "states": int(sum(n for (_, _, n) in blocks)), "npl": wl.npl,
+               "setup_s": round(setup_s, 1)}
+        evs = {}
+        for prec in ("mixed", "fp64") if with_fp64 else ("mixed",):
+            g = CyclixGPU(S, blocks, prec)
+            try:
+                for b, (_, _, n) in enumerate(blocks):
+                    g.set_psi(b, initial_psi(S.N, n, 900 + b))
+                EV = np.zeros(res["states"])
+                a0, bup, lc = np.zeros(nblk), np.zeros(nblk), np.zeros(nblk)
+                g.eigsolve(1, wl.npl, EV, a0, bup, lc)           # bounds (Lanczos) and first filter
+                g.sync()
+                if prec == "mixed":
+                    g.profile(True)
+                g.timer_start()
+                g.eigsolve(2, wl.npl, EV, a0, bup, lc)
+                ms = g.timer_stop()
+                res[f"{prec}_ms_per_step"] = round(ms, 2)
+                if prec == "mixed":
+                    n_l, kms, by = g.profile_read()
+                    g.profile(False)
+                    res["stencil_gbs"] = round(by / (kms * 1e-3) / 1e9, 1) if kms > 0 else None
+                evs[prec] = EV.copy()
+            finally:
+                g.close()
+        if "fp64" in evs:
+            off, err = 0, 0.0
+            for (_, _, n) in blocks:
+                err = max(err, float(np.max(np.abs(evs["mixed"][off:off + n // 2] - evs["fp64"][off:off + n // 2]))))
+                off += n
+            res["eig_err_lowest_half_ha"] = err
+            res["speedup_mixed_vs_fp64"] = round(res["fp64_ms_per_step"] / res["mixed_ms_per_step"], 2)
+        else:
+            res["fp64_ms_per_step"] = None
+            res["fp64_note"] = "not run: FP64 Rayleigh-Ritz of 8 x ~1000 states takes minutes per step on GB300 FP64"
+        if scf_cell:
+            # the full mixed-precision SCF to 1e-6 (src/scf.m) on this cell, from the atomic density
+            S.Veff = None
+            g = CyclixGPU(S, blocks, "mixed")
+            try:
+                for b, (_, _, n) in enumerate(blocks):
+                    g.set_psi(b, initial_psi(S.N, n, 900 + b))
+                t0 = time.perf_counter()
+                r, EV, rho, V, hist = g.scf(S, scf_tol=1e-6)
+                res["scf_mixed"] = {"n_scf": r.n_scf, "converged": bool(r.converged), "E_per_atom_ha": r.Etotal / S.n_atm,
+                                    "wall_s": round(time.perf_counter() - t0, 1)}
+            finally:
+                g.close()
+        print(json.dumps(res), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -254,6 +330,8 @@ def main():
                     help="profiling mode: time only the mixed-precision device-resident steps (no CPU baseline, FP64 arm or e2e)")
     ap.add_argument("--workload", default=WORKLOAD, help="workload name (profiling mode)")
     ap.add_argument("--ramp", type=int, default=6, help="untimed SCF ramp-up steps before the warm-up steps")
+    ap.add_argument("--configs", action="store_true",
+                    help="one eigSolver step of every workload (mixed and FP64) and the full mixed SCF of the 384-atom cell")
     args = ap.parse_args()
     warmup = max(3, args.warmup)
     rank = env_int("RANK", 0)
@@ -284,6 +362,10 @@ def main():
                 "e2e": {"value": round(v, 3), "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
                 "note": "the reference is MATLAB (not installable here); this arm times the NumPy/SciPy restatement of it"}
         print(json.dumps(line), flush=True)
+        return 0
+
+    if args.configs:
+        config_lines()
         return 0
 
     if args.only_mixed:
