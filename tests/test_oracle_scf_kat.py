@@ -1,0 +1,85 @@
+"""Known-answer tests of the oracle's SCF pieces (no GPU): the AAR solver (src/aar.m), the Poisson
+operator (src/poissonSolve.m, src/initialization.m:734-752), LDA_PW (src/exchangeCorrelationPotential.m,
+src/evaluateTotalEnergy.m), Gaussian-smearing occupations (src/occupations.m) and Periodic Pulay
+mixing (src/mixing.m, src/andersonWtdAvg.m)."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+from kat_systems import bare_cell
+from oracle import scf as OS
+
+
+def test_aar_solves_a_nonsymmetric_system():
+    rng = np.random.default_rng(0)
+    n = 200
+    A = sp.diags([np.full(n - 1, -1.0), np.full(n, 4.0), np.full(n - 1, -1.3)], [-1, 0, 1]).tocsr()
+    b = rng.standard_normal(n)
+    x, relres, it = OS.aar(A, b, None, 1e-10, 500, 0.6, 0.6, 7, 6, lambda r: r / 4.0)
+    assert relres <= 1e-10
+    assert np.max(np.abs(x - spla.spsolve(A.tocsc(), b))) < 1e-8
+
+
+def test_poisson_operator_recovers_a_potential():
+    S = bare_cell(17, 8, 12)
+    P = OS.PoissonOperator(S)
+    rng = np.random.default_rng(1)
+    phi0 = rng.standard_normal(S.N)
+    f = P.L @ phi0
+    phi, relres, it = P.solve(f, None, 1e-11)
+    assert relres <= 1e-11
+    assert np.max(np.abs(phi - phi0)) < 1e-7 * np.max(np.abs(phi0))
+
+
+@pytest.mark.parametrize("rho", [1e-4, 3e-3, 0.05, 0.7, 4.0])
+def test_lda_pw_potential_is_the_energy_derivative(rho):
+    # V_xc = d(rho eps_xc)/d rho: central difference of the energy density
+    W = np.ones(1)
+    h = 1e-6 * rho
+    e = lambda r: OS.lda_pw_energy(np.array([r]), W)
+    dnum = (e(rho + h) - e(rho - h)) / (2 * h)
+    v = OS.lda_pw_potential(np.array([rho]))[0]
+    assert abs(v - dnum) < 1e-6 * max(1.0, abs(v))
+
+
+def test_lda_pw_exchange_limit():
+    # high density: exchange dominates, eps_x = -(3/4)(3/pi)^(1/3) rho^(1/3)
+    rho = 1e4
+    ex = -0.75 * (3 / np.pi) ** (1 / 3) * rho ** (1 / 3)
+    exc = OS.lda_pw_energy(np.array([rho]), np.ones(1)) / rho
+    assert abs(exc - ex) / abs(ex) < 0.05
+
+
+def test_occupations_count_electrons():
+    rng = np.random.default_rng(2)
+    evs = [np.sort(rng.uniform(-1, 1, 20)), np.sort(rng.uniform(-1, 1, 18))]
+    wk = np.array([0.5, 0.5])
+    bet = 27.21138602 / 0.2
+    ne = 21.3
+    lam_f, occ = OS.occupations(evs, wk, bet, 2.0, -ne)
+    total = sum(2.0 * wk[k] * np.sum(occ[k]) for k in range(2))
+    assert abs(total - ne) < 1e-10
+    for o in occ:
+        assert np.all((o >= 0) & (o <= 1))
+    assert min(e.min() for e in evs) < lam_f < max(e.max() for e in evs)
+
+
+def test_periodic_pulay_finds_the_fixed_point():
+    # g(x) = M x + c with a contractive M: the fixed point solves (I - M) x = c
+    rng = np.random.default_rng(3)
+    n = 40
+    Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    M = Q @ np.diag(np.linspace(-0.8, 0.9, n)) @ Q.T
+    c = rng.standard_normal(n)
+    xs = np.linalg.solve(np.eye(n) - M, c)
+    mixer = OS.PeriodicPulay(n)
+    x = np.zeros(n)
+    for it in range(1, 60):
+        x = mixer(M @ x + c, x, it)
+    assert np.max(np.abs(x - xs)) < 1e-8 * np.max(np.abs(xs))
+    # simple mixing with the same parameter is far slower
+    y = np.zeros(n)
+    for it in range(1, 60):
+        y = y + 0.3 * (M @ y + c - y)
+    assert np.max(np.abs(y - xs)) > 1e-3 * np.max(np.abs(xs))
