@@ -95,6 +95,10 @@ def _make_workloads() -> dict:
     w["scf-small-24x12x20-12at-2k-ns40"] = Workload(
         "scf-small-24x12x20-12at-2k-ns40", 24, 12, 20, (40, 36),
         ((0.0, 0.0, 0.0), (0.0, 1.0, 0.0)), 1, 16, 12, 12, scf=True)
+    # small helical SCF used by the tests (twist 0.05 rad/bohr, one nu = 0 and one nu = 1, eta block)
+    w["scf-small-helical-24x12x16-8at-2k-ns28"] = Workload(
+        "scf-small-helical-24x12x16-8at-2k-ns28", 24, 12, 16, (28, 24),
+        ((0.0, 0.0, 0.0), (0.0, 1.0, 0.6)), 1, 16, 8, 12, twist=0.05, dz=0.25, scf=True)
     return w
 
 

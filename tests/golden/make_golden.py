@@ -91,9 +91,9 @@ def poisson_case() -> dict:
     return dict(phi=phi, relres=relres, iters=it)
 
 
-def scf_small() -> dict:
-    """The oracle SCF (src/scf.m) on the 24 x 12 x 20 12-atom cell, tol 1e-6, psi = initial_psi(N, Ns, 7 + b)."""
-    wl = WORKLOADS["scf-small-24x12x20-12at-2k-ns40"]
+def scf_small(name: str = "scf-small-24x12x20-12at-2k-ns40") -> dict:
+    """The oracle SCF (src/scf.m) on a small cell, tol 1e-6, psi = initial_psi(N, Ns, 7 + b)."""
+    wl = WORKLOADS[name]
     S = make_system(wl)
     bl = block_layout(wl, S)
     psis = [initial_psi(S.N, n, 7 + i) for i, (_, _, n) in enumerate(bl)]
@@ -112,6 +112,8 @@ def write_all(which=None):
         "eig_helical": lambda: (HERE / "eig_helical.json").write_text(json.dumps(eig_case("helical"), indent=1)),
         "poisson_cyclic": lambda: np.savez_compressed(HERE / "poisson_cyclic.npz", **poisson_case()),
         "scf_small": lambda: (HERE / "scf_small.json").write_text(json.dumps(scf_small(), indent=1)),
+        "scf_small_helical": lambda: (HERE / "scf_small_helical.json").write_text(
+            json.dumps(scf_small("scf-small-helical-24x12x16-8at-2k-ns28"), indent=1)),
     }
     for k, fn in jobs.items():
         if which is None or k in which:

@@ -1,4 +1,5 @@
-"""GPU SCF (cx_scf, src/scf.m) against the oracle SCF fixture on the 24 x 12 x 20 12-atom cell.
+"""GPU SCF (cx_scf, src/scf.m) against the oracle SCF fixtures: the cyclic 24 x 12 x 20 12-atom cell
+and the helical (twist 0.05 rad/bohr) 24 x 12 x 16 8-atom cell.
 
 Tolerances:
   * complex128: total energy within 1e-7 Ha/atom of the oracle, Fermi level within 1e-5 Ha and
@@ -20,16 +21,22 @@ pytestmark = pytest.mark.gpu
 GOLD = Path(__file__).resolve().parent / "golden"
 
 
-@pytest.fixture(scope="module")
-def scf_system():
-    wl = WORKLOADS["scf-small-24x12x20-12at-2k-ns40"]
+CASES = [("scf-small-24x12x20-12at-2k-ns40", "scf_small.json", 24),
+         ("scf-small-helical-24x12x16-8at-2k-ns28", "scf_small_helical.json", 16)]
+
+
+@pytest.fixture(scope="module", params=CASES, ids=[c[0] for c in CASES])
+def scf_system(request):
+    name, fixture, nocc = request.param
+    wl = WORKLOADS[name]
     S = make_system(wl)
-    return wl, S, block_layout(wl, S)
+    ref = json.loads((GOLD / fixture).read_text())
+    return wl, S, block_layout(wl, S), ref, nocc
 
 
 def _run(scf_system, prec):
     from cyclix_msparc_gb300.msparc import CyclixGPU
-    wl, S, bl = scf_system
+    wl, S, bl = scf_system[:3]
     g = CyclixGPU(S, bl, prec)
     try:
         for i, (_, _, n) in enumerate(bl):
@@ -40,18 +47,16 @@ def _run(scf_system, prec):
 
 
 def test_scf_fp64_matches_oracle(scf_system):
-    ref = json.loads((GOLD / "scf_small.json").read_text())
+    wl, S, bl, ref, nocc = scf_system
     res, EV, rho, V, hist = _run(scf_system, "fp64")
-    S = scf_system[1]
     assert res.converged == 1
     assert abs(res.Etotal / S.n_atm - ref["E_per_atom"]) < 1e-7
     assert abs(res.lambda_f - ref["lambda_f"]) < 1e-5
-    # occupied states (24 per block for 48 electrons over two equally weighted blocks); the top
-    # of each block converges slowest and is left out
+    # occupied states; the top of each block converges slowest and is left out
     off = 0
     for ev_ref in ref["EigVal"]:
         n = len(ev_ref)
-        assert np.max(np.abs(EV[off:off + 24] - np.array(ev_ref[:24]))) < 2e-5
+        assert np.max(np.abs(EV[off:off + nocc] - np.array(ev_ref[:nocc]))) < 2e-5
         off += n
     n = min(len(hist), len(ref["history"]))
     for (e, _), (_, er, _) in zip(hist[:n], ref["history"][:n]):
@@ -61,12 +66,11 @@ def test_scf_fp64_matches_oracle(scf_system):
 
 
 def test_scf_mixed_matches_oracle(scf_system):
-    ref = json.loads((GOLD / "scf_small.json").read_text())
+    wl, S, bl, ref, nocc = scf_system
     res, EV, rho, V, hist = _run(scf_system, "mixed")
-    S = scf_system[1]
     assert res.converged == 1
     assert abs(res.Etotal / S.n_atm - ref["E_per_atom"]) < 1e-6
     off = 0
     for ev_ref in ref["EigVal"]:
-        assert np.max(np.abs(EV[off:off + 24] - np.array(ev_ref[:24]))) < 2e-5
+        assert np.max(np.abs(EV[off:off + nocc] - np.array(ev_ref[:nocc]))) < 2e-5
         off += len(ev_ref)
