@@ -253,12 +253,14 @@ CONFIGS = [
 ]
 
 
-def config_lines():
+def config_lines(only=None):
     """One eigSolver step per configuration (mixed and, where it fits the run, FP64), plus the full
     mixed-precision SCF of the 384-atom cell.  One JSON line per configuration on stdout."""
     from cyclix_msparc_gb300.msparc import CyclixGPU
     from cyclix_msparc_gb300.workloads import WORKLOADS, block_layout, initial_psi, make_system
     for name, with_fp64 in CONFIGS:
+        if only and name != only:
+            continue
         wl = WORKLOADS[name]
         t0 = time.perf_counter()
         S = make_system(wl)
@@ -311,9 +313,10 @@ def config_lines():
                 for b, (_, _, n) in enumerate(blocks):
                     g.set_psi(b, initial_psi(S.N, n, 900 + b))
                 t0 = time.perf_counter()
-                r, EV, rho, V, hist = g.scf(S, scf_tol=1e-6)
+                r, EV, rho, V, hist = g.scf(S, scf_tol=1e-6, max_scf=40)
                 res["scf_mixed"] = {"n_scf": r.n_scf, "converged": bool(r.converged), "E_per_atom_ha": r.Etotal / S.n_atm,
-                                    "wall_s": round(time.perf_counter() - t0, 1)}
+                                    "wall_s": round(time.perf_counter() - t0, 1), "general_eig_solves": g.eig_fallbacks(),
+                                    "history_E_per_atom": [round(float(e), 10) for (e, _) in hist]}
             finally:
                 g.close()
         print(json.dumps(res), flush=True)
@@ -365,7 +368,7 @@ def main():
         return 0
 
     if args.configs:
-        config_lines()
+        config_lines(None if args.workload == WORKLOAD else args.workload)
         return 0
 
     if args.only_mixed:
