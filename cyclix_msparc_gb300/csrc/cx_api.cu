@@ -47,6 +47,8 @@ void free_blocks(cx_handle h) {
   cudaFree(h->d_state_tab); h->d_state_tab = nullptr;
   cudaFree(h->d_cprime); h->d_cprime = nullptr;
   cudaFree(h->d_seg_phase); h->d_seg_phase = nullptr;
+  cudaFree(h->d_seg_phase32); h->d_seg_phase32 = nullptr;
+  h->nl.seg_phase32 = nullptr;
   cudaFree(h->d_maps); h->d_maps = nullptr;
   h->nl.seg_phase = nullptr;
   h->nblk = 0;
@@ -295,9 +297,12 @@ static cx_status hpsi_T(cx_handle h, int blk, int ncol, const double* X, double*
   if ((s = dalloc(h, &v.d_scal, 1)) != CX_OK) return s;
   CX_TRY_CUDA(h, cudaMemcpy(v.d_scal, &one, sizeof(one), cudaMemcpyHostToDevice));
   const double2* saved = h->nl.seg_phase;
+  const float2* saved32 = h->nl.seg_phase32;
   h->nl.seg_phase = v.d_ph;
+  h->nl.seg_phase32 = nullptr;
   s = fused_step<R>(h, v.d_blk, v.d_scal, 1, v.d_tab, ncol, 0, false, v.cprime, true, 2.0 * n * sizeof(cplx<R>), v.d_maps ? &v.set : nullptr);
   h->nl.seg_phase = saved;
+  h->nl.seg_phase32 = saved32;
   if (s != CX_OK) return s;
   if ((s = check_pipeline_status(h)) != CX_OK) return s;
   return cx_dev_to_host(h, v.b1, Y, n, sizeof(R) == 8 ? CX_PREC_FP64 : CX_PREC_MIXED);
@@ -312,7 +317,9 @@ static cx_status filter_T(cx_handle h, int blk, int ncol, const double* X, doubl
   const int pr = sizeof(R) == 8 ? CX_PREC_FP64 : CX_PREC_MIXED;
   if ((s = cx_host_to_dev(h, X, v.b0, n, pr)) != CX_OK) return s;
   const double2* saved = h->nl.seg_phase;
+  const float2* saved32 = h->nl.seg_phase32;
   h->nl.seg_phase = v.d_ph;
+  h->nl.seg_phase32 = nullptr;
   StepScalars* saved_scal = h->d_scal;
   int saved_cap = h->scal_cap;
   h->d_scal = nullptr;
@@ -325,6 +332,7 @@ static cx_status filter_T(cx_handle h, int blk, int ncol, const double* X, doubl
   h->d_scal = saved_scal;
   h->scal_cap = saved_cap;
   h->nl.seg_phase = saved;
+  h->nl.seg_phase32 = saved32;
   if (s != CX_OK) return s;
   return cx_dev_to_host(h, sel ? v.b1 : v.b0, Y, n, pr);
 }
@@ -648,6 +656,17 @@ cx_status cx_set_blocks(cx_handle h, int32_t nblk, const cx_block* blocks, int32
   if ((s = dalloc(h, &h->d_seg_phase, ph.size())) != CX_OK) { free_blocks(h); return s; }
   CX_TRY_CUDA(h, cudaMemcpy(h->d_seg_phase, ph.data(), sizeof(double2) * ph.size(), cudaMemcpyHostToDevice));
   h->nl.seg_phase = h->d_seg_phase;
+  {
+    std::vector<float2> ph32(ph.size());
+    for (size_t i = 0; i < ph.size(); ++i) ph32[i] = make_float2((float)ph[i].x, (float)ph[i].y);
+    if (cudaMalloc(&h->d_seg_phase32, sizeof(float2) * std::max<size_t>(1, ph32.size())) != cudaSuccess) {
+      h->err = "cx_set_blocks: device memory for the segment phases";
+      free_blocks(h);
+      return CX_ERR_NOMEM;
+    }
+    CX_TRY_CUDA(h, cudaMemcpy(h->d_seg_phase32, ph32.data(), sizeof(float2) * ph32.size(), cudaMemcpyHostToDevice));
+    h->nl.seg_phase32 = h->d_seg_phase32;
+  }
   std::vector<int> ids(nblk);
   for (int b = 0; b < nblk; ++b) ids[b] = b;
   if (prec == CX_PREC_FP64) {

@@ -74,6 +74,7 @@ struct NonlocalDev {
   const int32_t* ent_seg;                    // entries: segment id
   const void* ent_chi;                       // entries x angmax real: Chi
   const double2* seg_phase;                  // nblk x nseg: exp(i k.(R_J - R_img)) per block
+  const float2* seg_phase32;                 // the same in float for the complex64 path (or null)
 };
 
 constexpr int kAngMax = 4;   // l <= 1 projectors: (lmax+1)^2 = 4 columns per atom at most
@@ -151,6 +152,7 @@ struct cx_handle_s {
   void* d_node_wchi64 = nullptr;
   void* d_ent_chi64 = nullptr;
   double2* d_seg_phase = nullptr;
+  float2* d_seg_phase32 = nullptr;
 
   // blocks
   int nblk = 0;

@@ -902,9 +902,12 @@ cx_status refine_eigenvalues(cx_handle h, double* EigVal) {
     cudaMemcpyAsync(d_sc, &one, sizeof(one), cudaMemcpyHostToDevice, h->stream);
     cudaMemcpyAsync(d_ph, ph.data(), ph.size() * sizeof(double2), cudaMemcpyHostToDevice, h->stream);
     const double2* saved = h->nl.seg_phase;
+    const float2* saved32 = h->nl.seg_phase32;
     h->nl.seg_phase = d_ph;
+    h->nl.seg_phase32 = nullptr;
     s = fused_step<double>(h, d_blk, d_sc, 1, d_tab, n, 0, false, cp, true, 0.0, nullptr);
     h->nl.seg_phase = saved;
+    h->nl.seg_phase32 = saved32;
     if (s != CX_OK) break;
     k_w_rq<<<n, 256, 0, h->stream>>>(A, HA, h->d_W, N, lam);
     h->launches++;

@@ -91,6 +91,7 @@ cx_status hpsi_noalloc_T(cx_handle h, int blk, int ncol, const void* X, void* Y,
   CX_TRY_CUDA(h, cudaMemcpyAsync(d_ph, ph.data(), sizeof(double2) * ph.size(), cudaMemcpyHostToDevice, st));
   NonlocalDev nl = h->nl;
   nl.seg_phase = d_ph;
+  nl.seg_phase32 = nullptr;
   nl.node_wchi = sizeof(R) == 4 ? h->d_node_wchi32 : h->d_node_wchi64;
   nl.ent_chi = sizeof(R) == 4 ? h->d_ent_chi32 : h->d_ent_chi64;
   const bool nonlocal = nl.nseg > 0;

@@ -222,11 +222,16 @@ nl_contract_kernel(const int N, const int nstates, const BlockDev<R>* __restrict
   const int nst = min(NC_SPC, nstates - gs0);
   const cplx<R>* y[NC_SPC];
   const double2* ph[NC_SPC];
+  const float2* ph32[NC_SPC];
+  // complex64 path: float phases (a double->float conversion per node and state costs more than
+  // the loads on GB300's narrow FP64 pipe)
+  const bool f32ph = sizeof(R) == 4 && nl.seg_phase32 != nullptr;
 #pragma unroll
   for (int j = 0; j < NC_SPC; ++j) {
     const int2 bs = state_tab[gs0 + (j < nst ? j : 0)];
     y[j] = blocks[bs.x].buf[in_sel] + (size_t)bs.y * N;
     ph[j] = nl.seg_phase + (size_t)bs.x * nl.nseg;
+    ph32[j] = f32ph ? nl.seg_phase32 + (size_t)bs.x * nl.nseg : nullptr;
   }
   const int n0 = nl.atom_node_ptr[J], n1 = nl.atom_node_ptr[J + 1];
   R a[NC_SPC][2 * kAngMax];
@@ -245,9 +250,18 @@ nl_contract_kernel(const int N, const int nstates, const BlockDev<R>* __restrict
     for (int j = 0; j < NC_SPC; ++j) {
       if (j < nst) {
         const cplx<R> v = y[j][pos];
-        const double2 p = ph[j][sg];
-        const R vx = v.x * (R)p.x - v.y * (R)p.y;
-        const R vy = v.x * (R)p.y + v.y * (R)p.x;
+        R px, py;
+        if (f32ph) {
+          const float2 p = ph32[j][sg];
+          px = (R)p.x;
+          py = (R)p.y;
+        } else {
+          const double2 p = ph[j][sg];
+          px = (R)p.x;
+          py = (R)p.y;
+        }
+        const R vx = v.x * px - v.y * py;
+        const R vy = v.x * py + v.y * px;
 #pragma unroll
         for (int q = 0; q < kAngMax; ++q) {
           a[j][2 * q] = fma(wq[q], vx, a[j][2 * q]);
