@@ -415,6 +415,10 @@ cx_status cx_create(const cx_grid* grid, int32_t n_atm, const cx_atom* atoms, in
   }
   cx_status s;
   if ((s = upload(h, &h->d_W, h->W)) != CX_OK) { g_create_err = h->err; cx_destroy(h); return s; }
+  {
+    const std::vector<float> w32(h->W.begin(), h->W.end());
+    if ((s = upload(h, &h->d_W32, w32)) != CX_OK) { g_create_err = h->err; cx_destroy(h); return s; }
+  }
   if ((s = dalloc(h, &h->d_veff, (size_t)N * nspin)) != CX_OK) { g_create_err = h->err; cx_destroy(h); return s; }
   if ((s = dalloc(h, &h->d_status, 1)) != CX_OK) { g_create_err = h->err; cx_destroy(h); return s; }
   CX_TRY_CUDA(h, cudaMemset(h->d_status, 0, sizeof(int)));

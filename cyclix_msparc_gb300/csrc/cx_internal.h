@@ -138,6 +138,7 @@ struct cx_handle_s {
   cx::StencilCoef coef{};
   std::vector<double> W;      // host copy
   double* d_W = nullptr;
+  float* d_W32 = nullptr;                            // float copy of W for the complex64 kernels
   int nspin = 1;
   double* d_veff = nullptr;   // N x nspin
 

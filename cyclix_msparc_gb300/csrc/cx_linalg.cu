@@ -45,32 +45,60 @@ static cx_status ensure(cx_handle h, void** p, size_t* cap, size_t bytes) {
 }
 
 // ------------------------------------------------------------------ W-normalisation (:122-124)
+// The complex64 kernels read a float copy of W: a double-to-float conversion per element runs on
+// GB300's narrow FP64 pipe.  Columns are indexed by blockIdx.y (no per-element division).
+template <typename R> struct WOf;
+template <> struct WOf<float> { using T = float; };
+template <> struct WOf<double> { using T = double; };
+
 template <typename R>
-__global__ void k_colnorm_w(const cplx<R>* __restrict__ X, const double* __restrict__ W, int N, double* __restrict__ out) {
+__global__ void k_colnorm_w(const cplx<R>* __restrict__ X, const typename WOf<R>::T* __restrict__ W, int N, double* __restrict__ out) {
   const cplx<R>* x = X + (size_t)blockIdx.x * N;
-  double acc = 0;
+  // per-thread compensated sum in the working precision, then the block reduction in double
+  R s = 0, comp = 0;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     const cplx<R> v = x[i];
-    acc += W[i] * ((double)v.x * v.x + (double)v.y * v.y);
+    const R term = W[i] * (v.x * v.x + v.y * v.y) - comp;
+    const R t = s + term;
+    comp = (t - s) - term;
+    s = t;
   }
+  double acc = (double)s;
   __shared__ double red[32];
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double s = 0;
-    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += red[k];
-    out[blockIdx.x] = 1.0 / sqrt(s);
+    double t = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+    out[blockIdx.x] = 1.0 / sqrt(t);
   }
 }
 template <typename R>
 __global__ void k_colscale(cplx<R>* __restrict__ X, int N, int ncol, const double* __restrict__ sc) {
-  const size_t n = (size_t)N * ncol;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const R s = (R)sc[i / N];
-    X[i].x *= s;
-    X[i].y *= s;
+  for (int col = blockIdx.y; col < ncol; col += gridDim.y) {
+    const R s = (R)sc[col];
+    cplx<R>* x = X + (size_t)col * N;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+      x[i].x *= s;
+      x[i].y *= s;
+    }
   }
+}
+template <typename R>
+__global__ void k_wscale(const cplx<R>* __restrict__ X, cplx<R>* __restrict__ Y, const typename WOf<R>::T* __restrict__ W, int N, int n) {
+  for (int col = blockIdx.y; col < n; col += gridDim.y) {
+    const cplx<R>* x = X + (size_t)col * N;
+    cplx<R>* y = Y + (size_t)col * N;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+      const R w = W[i];
+      y[i].x = x[i].x * w;
+      y[i].y = x[i].y * w;
+    }
+  }
+}
+static dim3 col_grid(int N, int n) {
+  return dim3((unsigned)std::min(64, (N + 255) / 256), (unsigned)std::min(n, 65535));
 }
 
 // gather columns: out[:, j] = in[:, perm[j]]
@@ -84,15 +112,6 @@ __global__ void k_gather_cols(const double2* __restrict__ in, double2* __restric
 
 // ------------------------------------------------------------------ subspace eigensolver kernels
 // WX = W .* X (column-major N x n)
-template <typename R>
-__global__ void k_wscale(const cplx<R>* __restrict__ X, cplx<R>* __restrict__ Y, const double* __restrict__ W, int N, int n) {
-  const size_t tot = (size_t)N * n;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
-    const R w = (R)W[i % N];
-    Y[i].x = X[i].x * w;
-    Y[i].y = X[i].y * w;
-  }
-}
 // Th = (T + T^H) / 2
 __global__ void k_herm_part(const double2* __restrict__ T, double2* __restrict__ Th, int n) {
   const size_t tot = (size_t)n * n;
@@ -666,7 +685,7 @@ static cx_status rayleigh_ritz_block(cx_handle h, int b, int sel, RRWork& w, dou
   cx_status s = rr_gemms<R>(h, X, HX, N, n, w);
   if (s != CX_OK) return s;
   // W-weighted Gram (needed by the subspace eigensolver): Gw = X^H (W X), W X in the H X buffer
-  k_wscale<R><<<grid_for((size_t)N * n), 256, 0, h->stream>>>(X, HX, h->d_W, N, n);
+  k_wscale<R><<<col_grid(N, n), 256, 0, h->stream>>>(X, HX, (const typename WOf<R>::T*)(sizeof(R) == 4 ? (const void*)h->d_W32 : (const void*)h->d_W), N, n);
   h->launches++;
   if ((s = rr_gram(h, X, HX, N, n, w)) != CX_OK) return s;
   // Cholesky G = R^H R (upper)
@@ -719,8 +738,9 @@ static cx_status rayleigh_ritz_block(cx_handle h, int b, int sel, RRWork& w, dou
   CX_TRY_CUDA(h, cudaMemcpyAsync(w.V, w.Hs, (size_t)n * n * 16, cudaMemcpyDeviceToDevice, h->stream));
   // psi = X C  (into the other buffer), then W-normalise (eigSolver.m:119-124)
   if ((s = rr_rotate<R>(h, X, HX, N, n, w)) != CX_OK) return s;
-  k_colnorm_w<R><<<n, 256, 0, h->stream>>>(HX, h->d_W, N, w.scfac);
-  k_colscale<R><<<grid_for((size_t)N * n), 256, 0, h->stream>>>(HX, N, n, w.scfac);
+  k_colnorm_w<R><<<n, 256, 0, h->stream>>>(HX, (const typename WOf<R>::T*)(sizeof(R) == 4 ? (const void*)h->d_W32 : (const void*)h->d_W), N,
+                                          w.scfac);
+  k_colscale<R><<<col_grid(N, n), 256, 0, h->stream>>>(HX, N, n, w.scfac);
   h->launches += 2;
   CX_TRY_CUDA(h, cudaGetLastError());
   return CX_OK;
