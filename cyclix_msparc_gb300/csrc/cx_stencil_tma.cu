@@ -411,16 +411,15 @@ __global__ void __launch_bounds__(TM_MAXW * 32, 1) cheb_tma_kernel(const __grid_
 
 // ---------------------------------------------------------------------------------- host side
 static PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
+  // looked up once (thread-safe static initialisation)
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
     void* p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
-  }
+      return (PFN_cuTensorMapEncodeTiled_v12000)p;
+    return nullptr;
+  }();
   return fn;
 }
 
@@ -544,11 +543,9 @@ cudaError_t launch_cheb_step_tma(const GridDev& g, const StencilCoef& coef, cons
   a.ostage_bytes = t.ostage_bytes;
   a.nos = t.nos;
   // one CTA per SM at a time: whole-z items fill full waves, the remainder is split along z
-  static int nsm = 0;
-  if (nsm == 0) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) nsm = 1;
-  }
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm < 1)
+    nsm = 1;
   const long items = (long)a.tiles_r * t.tiles_t * nstates;
   const long rem = items % nsm;
   a.zsplit = 1;
