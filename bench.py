@@ -253,7 +253,7 @@ CONFIGS = [
 ]
 
 
-def config_lines(only=None):
+def config_lines(only=None, max_scf=40, skip_steps=False):
     """One eigSolver step per configuration (mixed and, where it fits the run, FP64), plus the full
     mixed-precision SCF of the 384-atom cell.  One JSON line per configuration on stdout."""
     from cyclix_msparc_gb300.msparc import CyclixGPU
@@ -273,7 +273,7 @@ def config_lines(only=None):
         res = {"workload": name, "N": S.N, "blocks": nblk, "states": int(sum(n for (_, _, n) in blocks)), "npl": wl.npl,
                "setup_s": round(setup_s, 1)}
         evs = {}
-        for prec in ("mixed", "fp64") if with_fp64 else ("mixed",):
+        for prec in (() if skip_steps else (("mixed", "fp64") if with_fp64 else ("mixed",))):
             g = CyclixGPU(S, blocks, prec)
             try:
                 for b, (_, _, n) in enumerate(blocks):
@@ -295,7 +295,9 @@ def config_lines(only=None):
                 evs[prec] = EV.copy()
             finally:
                 g.close()
-        if "fp64" in evs:
+        if skip_steps:
+            pass
+        elif "fp64" in evs:
             off, err = 0, 0.0
             for (_, _, n) in blocks:
                 err = max(err, float(np.max(np.abs(evs["mixed"][off:off + n // 2] - evs["fp64"][off:off + n // 2]))))
@@ -313,8 +315,9 @@ def config_lines(only=None):
                 for b, (_, _, n) in enumerate(blocks):
                     g.set_psi(b, initial_psi(S.N, n, 900 + b))
                 t0 = time.perf_counter()
-                r, EV, rho, V, hist = g.scf(S, scf_tol=1e-6, max_scf=40)
+                r, EV, rho, V, hist = g.scf(S, scf_tol=1e-6, max_scf=max_scf)
                 res["scf_mixed"] = {"n_scf": r.n_scf, "converged": bool(r.converged), "E_per_atom_ha": r.Etotal / S.n_atm,
+                                    "err": r.err,
                                     "wall_s": round(time.perf_counter() - t0, 1), "general_eig_solves": g.eig_fallbacks(),
                                     "history_E_per_atom": [round(float(e), 10) for (e, _) in hist]}
             finally:
@@ -333,6 +336,8 @@ def main():
                     help="profiling mode: time only the mixed-precision device-resident steps (no CPU baseline, FP64 arm or e2e)")
     ap.add_argument("--workload", default=WORKLOAD, help="workload name (profiling mode)")
     ap.add_argument("--ramp", type=int, default=6, help="untimed SCF ramp-up steps before the warm-up steps")
+    ap.add_argument("--max-scf", type=int, default=40, help="SCF step limit of the full-SCF configuration (--configs)")
+    ap.add_argument("--scf-only", action="store_true", help="--configs: only the full SCF of the SCF cell")
     ap.add_argument("--configs", action="store_true",
                     help="one eigSolver step of every workload (mixed and FP64) and the full mixed SCF of the 384-atom cell")
     args = ap.parse_args()
@@ -368,7 +373,7 @@ def main():
         return 0
 
     if args.configs:
-        config_lines(None if args.workload == WORKLOAD else args.workload)
+        config_lines(None if args.workload == WORKLOAD else args.workload, args.max_scf, args.scf_only)
         return 0
 
     if args.only_mixed:

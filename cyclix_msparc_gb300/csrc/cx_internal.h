@@ -198,6 +198,7 @@ struct cx_handle_s {
   double prof_ms = 0, prof_bytes = 0, prof_apply_ms = 0;
   int64_t launches = 0;
   int64_t eig_fallbacks = 0;                         // subspace eigensolves that needed the general solver
+  int64_t eig_restarts = 0;                          // similarity restarts of the eigenvector refinement
 };
 
 #define CX_TRY_CUDA(h, expr)                                                                 \

@@ -112,6 +112,10 @@ __global__ void k_gather_cols(const double2* __restrict__ in, double2* __restric
 
 // ------------------------------------------------------------------ subspace eigensolver kernels
 // WX = W .* X (column-major N x n)
+// X += I
+__global__ void k_add_identity(double2* __restrict__ X, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) X[(size_t)i * n + i].x += 1.0;
+}
 // Th = (T + T^H) / 2
 __global__ void k_herm_part(const double2* __restrict__ T, double2* __restrict__ Th, int n) {
   const size_t tot = (size_t)n * n;
@@ -391,6 +395,8 @@ static cx_status lanczos_bounds(cx_handle h, int K, std::vector<double>& lmin, s
     }                                                                                 \
   } while (0)
 
+constexpr int kRestarts = 4;      // similarity restarts of a stalled refinement before the general solver
+
 struct RRWork {
   double2 *G, *Hs, *V, *ev;
   double2 *Gw, *T, *U, *B, *Z, *Zn, *EZ, *Hs0;   // subspace eigensolver (W-similarity + refinement)
@@ -399,11 +405,13 @@ struct RRWork {
   double* scfac;
   int* perm;
   int* info;
+  double2* Zbest;            // best iterate of a stalled refinement (restart point)
+  int64_t* ipiv;             // LU pivots of a restart
 };
 
 static cx_status rr_workspace(cx_handle h, int nmax, int ncolmax, RRWork& w) {
   const size_t n2 = (size_t)nmax * nmax;
-  const size_t need = n2 * 16 * 11 + nmax * 16 + nmax * 8 + 64 + n2 * 8 * 3 + (size_t)ncolmax * 8 + nmax * 4 + 64 + 32 * 256;
+  const size_t need = n2 * 16 * 12 + nmax * 16 + nmax * 8 + 64 + n2 * 8 * 3 + (size_t)ncolmax * 8 + nmax * 4 + 64 + nmax * 8 + 40 * 256;
   cx_status s = ensure(h, &h->d_rr, &h->rr_bytes, need);
   if (s != CX_OK) return s;
   char* p = (char*)h->d_rr;
@@ -428,6 +436,8 @@ static cx_status rr_workspace(cx_handle h, int nmax, int ncolmax, RRWork& w) {
   w.scfac = (double*)take((size_t)ncolmax * 8);
   w.perm = (int*)take(nmax * 4);
   w.info = (int*)take(64);
+  w.Zbest = (double2*)take(n2 * 16);
+  w.ipiv = (int64_t*)take((size_t)nmax * 8);
   return CX_OK;
 }
 
@@ -552,8 +562,10 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, bool* used_fallback
   // The mixed path runs the first sweeps with the B Z product on the tensor cores (complex64
   // operands, FP32-accurate BF16x9 products) down to the FP32 level, then finishes in complex128.
   const bool mixed = h->prec == CX_PREC_MIXED;
+  double best_dm = 1e300;   // best step size of the last refine() call; its iterate is in w.Zbest
   auto refine = [&](bool* conv) -> cx_status {
     *conv = false;
+    best_dm = 1e300;
     k_split_diag<<<gn, 256, 0, st>>>(w.B, w.ev, w.Z, n);
     h->launches++;
     bool fp32 = mixed;
@@ -584,6 +596,10 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, bool* used_fallback
       CX_TRY_CUDA(h, cudaMemcpyAsync(&dm, w.dmax, 8, cudaMemcpyDeviceToHost, st));
       CX_TRY_CUDA(h, cudaStreamSynchronize(st));
       if (!(dm < 1e300)) return CX_OK;                       // diverged (inf / NaN)
+      if (dm < best_dm) {
+        best_dm = dm;
+        CX_TRY_CUDA(h, cudaMemcpyAsync(w.Zbest, w.Z, n2 * 16, cudaMemcpyDeviceToDevice, st));
+      }
       if (fp32) {
         // FP32 level reached (or the complex64 sweeps stall): continue in complex128
         if (dm < 1e-6 || (it >= 8 && dm > 0.9 * prev)) { fp32 = false; prev = 1e300; }
@@ -633,14 +649,54 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, bool* used_fallback
     CX_TRY_CUDA(h, cudaMemcpyAsync(&info, w.info, sizeof(int), cudaMemcpyDeviceToHost, st));
     CX_TRY_CUDA(h, cudaStreamSynchronize(st));
     if (info == 0) {
-      if ((rs = refine(&conv)) != CX_OK) return rs;
-      if (conv) {
-        // eigenvectors of A: c = U_w^-1 (U X)
-        CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, (const cuDoubleComplex*)w.U, n,
-                                   (const cuDoubleComplex*)w.Z, n, &zero, (cuDoubleComplex*)w.V, n));
-        CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
-                                   (const cuDoubleComplex*)w.Gw, n, (cuDoubleComplex*)w.V, n));
-        return CX_OK;
+      // B X = X Lambda by the fixed point; when it stalls, restart from the similar matrix
+      // X^-1 B X with X = I + Z of the best iterate (each restart shrinks the coupling
+      // quadratically), accumulating the transforms in Xt (w.V, starting at U).  Bfull (w.T; T is
+      // no longer needed) keeps the matrix of the current round, since refine() splits w.B.
+      CX_TRY_CUDA(h, cudaMemcpyAsync(w.T, w.B, n2 * 16, cudaMemcpyDeviceToDevice, st));
+      CX_TRY_CUDA(h, cudaMemcpyAsync(w.V, w.U, n2 * 16, cudaMemcpyDeviceToDevice, st));
+      for (int round = 0; round <= kRestarts; ++round) {
+        if (round > 0) CX_TRY_CUDA(h, cudaMemcpyAsync(w.B, w.T, n2 * 16, cudaMemcpyDeviceToDevice, st));
+        if ((rs = refine(&conv)) != CX_OK) return rs;
+        if (conv) {
+          // eigenvectors of A: c = U_w^-1 (Xt X)
+          CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, (const cuDoubleComplex*)w.V, n,
+                                     (const cuDoubleComplex*)w.Z, n, &zero, (cuDoubleComplex*)w.Hs, n));
+          CX_TRY_CUDA(h, cudaMemcpyAsync(w.V, w.Hs, n2 * 16, cudaMemcpyDeviceToDevice, st));
+          CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n,
+                                     &one, (const cuDoubleComplex*)w.Gw, n, (cuDoubleComplex*)w.V, n));
+          h->eig_restarts += round;
+          return CX_OK;
+        }
+        if (round == kRestarts || !(best_dm < 1.0)) break;
+        // X = I + Z_best;  Bfull <- X^-1 (Bfull X);  Xt <- Xt X
+        k_add_identity<<<gn, 256, 0, st>>>(w.Zbest, n);
+        h->launches++;
+        CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, (const cuDoubleComplex*)w.T, n,
+                                   (const cuDoubleComplex*)w.Zbest, n, &zero, (cuDoubleComplex*)w.Hs, n));
+        CX_TRY_CUDA(h, cudaMemcpyAsync(w.EZ, w.Zbest, n2 * 16, cudaMemcpyDeviceToDevice, st));
+        size_t lwd = 0, lwh = 0;
+        CX_TRY_SOLVER(h, cusolverDnXgetrf_bufferSize(h->cusolver, h->cusolver_params, n, n, CUDA_C_64F, w.EZ, n, CUDA_C_64F, &lwd,
+                                                      &lwh));
+        if ((s = ensure(h, &h->d_ws, &h->ws_bytes, lwd + 256)) != CX_OK) return s;
+        if (h->hws_bytes < lwh + 256) {
+          cudaFreeHost(h->h_ws);
+          h->h_ws = nullptr;
+          h->hws_bytes = 0;
+          CX_TRY_CUDA(h, cudaMallocHost(&h->h_ws, lwh + 256));
+          h->hws_bytes = lwh + 256;
+        }
+        CX_TRY_SOLVER(h, cusolverDnXgetrf(h->cusolver, h->cusolver_params, n, n, CUDA_C_64F, w.EZ, n, w.ipiv, CUDA_C_64F, h->d_ws,
+                                           h->ws_bytes, h->h_ws, h->hws_bytes, w.info));
+        CX_TRY_SOLVER(h, cusolverDnXgetrs(h->cusolver, h->cusolver_params, CUBLAS_OP_N, n, n, CUDA_C_64F, w.EZ, n, w.ipiv, CUDA_C_64F,
+                                           w.Hs, n, w.info));
+        CX_TRY_CUDA(h, cudaMemcpyAsync(&info, w.info, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CX_TRY_CUDA(h, cudaStreamSynchronize(st));
+        if (info != 0) break;                                   // singular transform: general solver
+        CX_TRY_CUDA(h, cudaMemcpyAsync(w.T, w.Hs, n2 * 16, cudaMemcpyDeviceToDevice, st));
+        CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, (const cuDoubleComplex*)w.V, n,
+                                   (const cuDoubleComplex*)w.Zbest, n, &zero, (cuDoubleComplex*)w.Hs, n));
+        CX_TRY_CUDA(h, cudaMemcpyAsync(w.V, w.Hs, n2 * 16, cudaMemcpyDeviceToDevice, st));
       }
     }
   }
