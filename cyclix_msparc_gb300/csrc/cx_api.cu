@@ -1,5 +1,9 @@
-// C-ABI entry points of libcyclix_gpu.so: handle lifecycle, operator tables, block
-// buffers, host <-> device transfers, H*psi and the Chebyshev filter.
+// C-ABI entry points of libcyclix_gpu.so: handle lifecycle, operator tables (stencil
+// coefficients from Cychel/lapIndicesValues_1d_cychel.m, projector images in the layout of
+// calculate_nloc_projector.m), block buffers, host <-> device transfers, H*psi
+// (src/h_nonlocal_vector_mult.m) and the Chebyshev filter (src/chebyshev_filter.m).  One
+// Chebyshev step on the complex64 path is three launches: projector contraction, TMA stencil,
+// projector apply; on the complex128 path two (the apply is fused into the stencil).
 #include <cmath>
 #include <cstdio>
 #include <cstring>
