@@ -48,3 +48,47 @@ def test_null_handle_is_rejected(lib):
     assert lib.cx_hpsi(None, 0, 1, None, None, 0) == 1      # CX_ERR_ARG
     assert lib.cx_eigsolver(None, 1, 4, 4, None, None, None, None) == 1
     assert lib.cx_destroy(None) == 0
+
+
+def _grid(**kw):
+    import numpy as np
+    from cyclix_msparc_gb300 import _lib
+    from cyclix_msparc_gb300.cychel import fd_weights
+    w1, w2 = fd_weights(6)
+    keep = [np.ascontiguousarray(w1), np.ascontiguousarray(w2), np.ones(16 * 8 * 10)]
+    args = dict(Nx=16, Ny=8, Nz=10, FDn=6, cell_typ=3, BCx=1, BCy=0, BCz=0, dx=0.25, dy=0.06, dz=0.2, xin=4.0, twist=0.0,
+                L1=3.75, L2=0.52, L3=2.0)
+    args.update(kw)
+    g = _lib.cx_grid(**args)
+    g.w1 = _lib.dptr(keep[0])
+    g.w2 = _lib.dptr(keep[1])
+    g.W = _lib.dptr(keep[2])
+    return g, keep
+
+
+@pytest.mark.parametrize("bad,msg", [
+    (dict(FDn=0), "FDn"),
+    (dict(cell_typ=2), "cell_typ"),
+    (dict(BCx=0), "Dirichlet"),
+    (dict(Ny=6), "Ny, Nz > FDn"),
+    (dict(cell_typ=5, twist=0.0), "twist"),
+])
+def test_create_rejects_bad_grids_without_cuda(lib, bad, msg):
+    # argument checks come before any CUDA call, so they run on a machine without a GPU
+    import ctypes as C
+    g, keep = _grid(**bad)
+    h = C.c_void_p()
+    st = lib.cx_create(C.byref(g), 0, None, 1, C.byref(h))
+    assert st == 1 and not h.value
+    assert msg in lib.cx_last_error(None).decode()
+
+
+def test_create_rejects_bad_spin_and_atoms(lib):
+    import ctypes as C
+    g, keep = _grid()
+    h = C.c_void_p()
+    assert lib.cx_create(C.byref(g), 0, None, 3, C.byref(h)) == 1
+    assert "nspin" in lib.cx_last_error(None).decode()
+    assert lib.cx_create(C.byref(g), 2, None, 1, C.byref(h)) == 1
+    assert "atoms" in lib.cx_last_error(None).decode()
+    assert lib.cx_create(None, 0, None, 1, C.byref(h)) == 1
