@@ -199,6 +199,7 @@ struct cx_handle_s {
   int64_t launches = 0;
   int64_t eig_fallbacks = 0;                         // subspace eigensolves that needed the general solver
   int64_t eig_restarts = 0;                          // similarity restarts of the eigenvector refinement
+  int restart_fail_streak = 0;                       // blocks in a row whose restarts ended in the general solver
 };
 
 #define CX_TRY_CUDA(h, expr)                                                                 \

@@ -399,6 +399,8 @@ static cx_status lanczos_bounds(cx_handle h, int K, std::vector<double>& lmin, s
   } while (0)
 
 constexpr int kRestarts = 4;      // similarity restarts of a stalled refinement before the general solver
+constexpr int kRestartGiveUp = 4; // blocks in a row that needed the general solver after restarts: stop
+                                  // restarting for the rest of the eigSolver call
 
 struct RRWork {
   double2 *G, *Hs, *V, *ev;
@@ -658,7 +660,8 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, bool* used_fallback
       // no longer needed) keeps the matrix of the current round, since refine() splits w.B.
       CX_TRY_CUDA(h, cudaMemcpyAsync(w.T, w.B, n2 * 16, cudaMemcpyDeviceToDevice, st));
       CX_TRY_CUDA(h, cudaMemcpyAsync(w.V, w.U, n2 * 16, cudaMemcpyDeviceToDevice, st));
-      for (int round = 0; round <= kRestarts; ++round) {
+      const int max_round = h->restart_fail_streak >= kRestartGiveUp ? 0 : kRestarts;
+      for (int round = 0; round <= max_round; ++round) {
         if (round > 0) CX_TRY_CUDA(h, cudaMemcpyAsync(w.B, w.T, n2 * 16, cudaMemcpyDeviceToDevice, st));
         if ((rs = refine(&conv)) != CX_OK) return rs;
         if (conv) {
@@ -669,9 +672,13 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, bool* used_fallback
           CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n,
                                      &one, (const cuDoubleComplex*)w.Gw, n, (cuDoubleComplex*)w.V, n));
           h->eig_restarts += round;
+          if (round > 0) h->restart_fail_streak = 0;
           return CX_OK;
         }
-        if (round == kRestarts || !(best_dm < 1.0)) break;
+        if (round == max_round || !(best_dm < 1.0)) {
+          if (round > 0) h->restart_fail_streak++;
+          break;
+        }
         // X = I + Z_best;  Bfull <- X^-1 (Bfull X);  Xt <- Xt X
         k_add_identity<<<gn, 256, 0, st>>>(w.Zbest, n);
         h->launches++;
@@ -695,7 +702,10 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, bool* used_fallback
                                            w.Hs, n, w.info));
         CX_TRY_CUDA(h, cudaMemcpyAsync(&info, w.info, sizeof(int), cudaMemcpyDeviceToHost, st));
         CX_TRY_CUDA(h, cudaStreamSynchronize(st));
-        if (info != 0) break;                                   // singular transform: general solver
+        if (info != 0) {                                        // singular transform: general solver
+          h->restart_fail_streak++;
+          break;
+        }
         CX_TRY_CUDA(h, cudaMemcpyAsync(w.T, w.Hs, n2 * 16, cudaMemcpyDeviceToDevice, st));
         CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, (const cuDoubleComplex*)w.V, n,
                                    (const cuDoubleComplex*)w.Zbest, n, &zero, (cuDoubleComplex*)w.Hs, n));
@@ -808,6 +818,7 @@ static cx_status rayleigh_ritz_block(cx_handle h, int b, int sel, RRWork& w, dou
 template <typename R>
 static cx_status eigsolver_T(cx_handle h, int count, int npl, int rhoTrigger, double* EigVal, double* a0, double* bup, double* lc) {
   const int nblk = h->nblk;
+  h->restart_fail_streak = 0;
   std::vector<int> off(nblk + 1, 0);
   for (int b = 0; b < nblk; ++b) off[b + 1] = off[b] + h->blocks[b].Ns;
   // ---- bounds and cutoff (eigSolver.m:47-94, first relaxation step)
