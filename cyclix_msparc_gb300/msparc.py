@@ -25,6 +25,22 @@ from ._lib import CxError, check, cptr, dptr
 __all__ = ["CyclixGPU", "attach", "h_nonlocal_vector_mult", "chebyshev_filter", "eigSolver", "poissonSolve", "scf", "CxError"]
 
 
+def _host_buffer(a, dtype, size: int, name: str) -> None:
+    """Check an array that the library reads or writes through a raw pointer: its dtype, one
+    contiguous block, at least ``size`` elements and, since the library writes into it, writable.
+    Anything else would make the library touch memory outside the array, so it raises
+    ``ValueError`` before the call (independently of ``python -O``)."""
+    if not isinstance(a, np.ndarray) or a.dtype != np.dtype(dtype):
+        got = a.dtype if isinstance(a, np.ndarray) else type(a).__name__
+        raise ValueError(f"{name}: need a numpy array of {np.dtype(dtype).name}, got {got}")
+    if not (a.flags.c_contiguous or a.flags.f_contiguous):
+        raise ValueError(f"{name}: the array must be one contiguous block")
+    if not a.flags.writeable:
+        raise ValueError(f"{name}: the array must be writable (the library updates it in place)")
+    if a.size < size:
+        raise ValueError(f"{name}: {a.size} elements, the library needs {size}")
+
+
 class CyclixGPU:
     """Owns one ``cx_handle``: the discretised operator of ``S`` and its Bloch blocks."""
 
@@ -87,11 +103,14 @@ class CyclixGPU:
 
     def set_veff(self, Veff):
         V = np.asfortranarray(np.asarray(Veff, dtype=np.float64).reshape(self.N, -1, order="F"))
+        if V.shape[1] != int(self.S.nspin):
+            raise ValueError(f"set_veff: need N x nspin = {self.N} x {int(self.S.nspin)} values, got {V.shape}")
         check(self.lib, self.h, self.lib.cx_set_veff(self.h, dptr(V)))
 
     def set_psi(self, blk, psi):
         a = np.asfortranarray(psi, dtype=np.complex128)
-        assert a.shape == (self.N, self.Ns[blk])
+        if a.shape != (self.N, self.Ns[blk]):
+            raise ValueError(f"set_psi: block {blk} is {self.N} x {self.Ns[blk]}, got {a.shape}")
         check(self.lib, self.h, self.lib.cx_set_psi(self.h, blk, cptr(a)))
 
     def get_psi(self, blk):
@@ -100,32 +119,43 @@ class CyclixGPU:
         return a
 
     # -- operators ---------------------------------------------------------------------------
-    def hpsi(self, blk, X, prec=None):
+    def _columns(self, X, name):
         X = np.asfortranarray(X, dtype=np.complex128)
         if X.ndim == 1:
             X = X[:, None]
+        if X.ndim != 2 or X.shape[0] != self.N:
+            raise ValueError(f"{name}: need N = {self.N} rows, got shape {X.shape}")
+        return X
+
+    def hpsi(self, blk, X, prec=None):
+        X = self._columns(X, "hpsi")
         Y = np.empty_like(X, order="F")
         check(self.lib, self.h, self.lib.cx_hpsi(self.h, blk, X.shape[1], cptr(X),
                                                  cptr(Y), _lib.PREC[prec or self.prec]))
         return Y
 
     def filter(self, blk, X, m, a, b, a0, prec=None):
-        X = np.asfortranarray(X, dtype=np.complex128)
+        X = self._columns(X, "filter")
         Y = np.empty_like(X, order="F")
         check(self.lib, self.h, self.lib.cx_chebyshev_filter(self.h, blk, X.shape[1], cptr(X),
                                                              cptr(Y), int(m), float(a), float(b), float(a0),
                                                              _lib.PREC[prec or self.prec]))
         return Y
 
+    def _check_step_arrays(self, EigVal, a0, bup, lambda_cutoff):
+        _host_buffer(EigVal, np.float64, int(sum(self.Ns)), "EigVal")
+        for name, v in (("a0", a0), ("bup", bup), ("lambda_cutoff", lambda_cutoff)):
+            _host_buffer(v, np.float64, len(self.blocks), name)
+
     def eigsolve(self, count, npl, EigVal, a0, bup, lambda_cutoff, rhoTrigger=4):
         """Device-resident eigSolver step: arrays are updated in place."""
-        for v in (EigVal, a0, bup, lambda_cutoff):
-            assert v.dtype == np.float64 and v.flags.c_contiguous
+        self._check_step_arrays(EigVal, a0, bup, lambda_cutoff)
         check(self.lib, self.h, self.lib.cx_eigsolver(self.h, int(count), int(npl), int(rhoTrigger), dptr(EigVal), dptr(a0),
                                                       dptr(bup), dptr(lambda_cutoff)))
 
     def eigsolve_host(self, count, npl, psi_packed, EigVal, a0, bup, lambda_cutoff, rhoTrigger=4):
-        assert psi_packed.dtype == np.complex128 and (psi_packed.flags.c_contiguous or psi_packed.flags.f_contiguous)
+        _host_buffer(psi_packed, np.complex128, self.N * int(sum(self.Ns)), "psi")
+        self._check_step_arrays(EigVal, a0, bup, lambda_cutoff)
         check(self.lib, self.h, self.lib.cx_eigsolver_host(self.h, int(count), int(npl), int(rhoTrigger),
                                                            cptr(psi_packed),
                                                            dptr(EigVal), dptr(a0), dptr(bup), dptr(lambda_cutoff)))
@@ -150,8 +180,10 @@ class CyclixGPU:
         return res, EV, rho, V, hist[: res.n_scf]
 
     def poisson(self, f, phi0=None, tol=1e-8, maxit=1000):
-        f = np.ascontiguousarray(f, dtype=np.float64)
-        phi = np.ascontiguousarray(phi0 if phi0 is not None else np.zeros(self.N), dtype=np.float64).copy()
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
+        phi = np.ascontiguousarray(phi0 if phi0 is not None else np.zeros(self.N), dtype=np.float64).reshape(-1).copy()
+        if f.size != self.N or phi.size != self.N:
+            raise ValueError(f"poisson: f and phi need N = {self.N} values, got {f.size} and {phi.size}")
         it = C.c_int32(0)
         rr = C.c_double(0)
         st = self.lib.cx_poisson(self.h, dptr(f), dptr(phi), float(tol), int(maxit), 1 if phi0 is not None else 0,

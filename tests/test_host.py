@@ -92,3 +92,36 @@ def test_initial_psi_orthonormal():
     X = initial_psi(500, 7, 3)
     assert np.allclose(X.conj().T @ X, np.eye(7), atol=1e-12)
     assert X.flags.f_contiguous
+
+
+def test_host_buffer_checks_reject_what_the_library_would_overrun():
+    # arrays handed to the C library by pointer are checked before the call (not by assert)
+    from cyclix_msparc_gb300.msparc import _host_buffer
+    _host_buffer(np.zeros(5), np.float64, 5, "EigVal")
+    _host_buffer(np.zeros((4, 3), dtype=np.complex128, order="F"), np.complex128, 12, "psi")
+    bad = [
+        (np.zeros(4), np.float64, 5, "elements"),                        # too short
+        (np.zeros(5, dtype=np.float32), np.float64, 5, "float64"),       # wrong dtype
+        ([0.0] * 5, np.float64, 5, "numpy array"),                       # not an array
+        (np.zeros(10)[::2], np.float64, 5, "contiguous"),                # strided view
+    ]
+    for a, dt, n, msg in bad:
+        with pytest.raises(ValueError, match=msg):
+            _host_buffer(a, dt, n, "x")
+    ro = np.zeros(5)
+    ro.setflags(write=False)
+    with pytest.raises(ValueError, match="writable"):
+        _host_buffer(ro, np.float64, 5, "x")
+
+
+def test_operator_inputs_need_n_rows():
+    # hpsi / filter read N x ncol values: other row counts are refused on the host
+    from cyclix_msparc_gb300.msparc import CyclixGPU
+    g = CyclixGPU.__new__(CyclixGPU)         # no handle: only the host-side check runs
+    g.N = 12
+    assert g._columns(np.ones(12), "hpsi").shape == (12, 1)
+    assert g._columns(np.ones((12, 3)), "hpsi").flags.f_contiguous
+    with pytest.raises(ValueError, match="N = 12 rows"):
+        g._columns(np.ones((11, 3)), "hpsi")
+    with pytest.raises(ValueError, match="N = 12 rows"):
+        g._columns(np.ones((12, 3, 2)), "filter")
