@@ -189,7 +189,9 @@ def cyclix_kpoints(nkpt, L1, L2, L3, kptshift=(0.0, 0.0, 0.0), time_reversal=Tru
     kz = np.mod(kz + 0.5 - eps, 1.0) - 0.5 + eps
     sumx, sumy, sumz = 0.0, 2 * np.pi / L2, 0.0
     kx = (2 * np.pi / L1) * kx
-    ky = np.round((2 * np.pi / L2) * ky)
+    # MATLAB's round (half away from zero; ky >= 0 here), not NumPy's round-half-to-even:
+    # an odd wedge order puts nu exactly on .5 (n_cyc = 5, 2 points: 2.5 -> 3)
+    ky = np.floor((2 * np.pi / L2) * ky + 0.5)
     kz = (2 * np.pi / L3) * kz
     KX, KY, KZ = np.meshgrid(kx, ky, kz, indexing="ij")
     kpt = np.stack([KX.reshape(-1, order="F"), KY.reshape(-1, order="F"), KZ.reshape(-1, order="F")], axis=1)

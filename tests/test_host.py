@@ -125,3 +125,11 @@ def test_operator_inputs_need_n_rows():
         g._columns(np.ones((11, 3)), "hpsi")
     with pytest.raises(ValueError, match="N = 12 rows"):
         g._columns(np.ones((12, 3, 2)), "filter")
+
+
+@pytest.mark.parametrize("n_cyc,expect", [(5, [0.0, 3.0]), (9, [0.0, 5.0]), (13, [0.0, 7.0])])
+def test_cyclix_kpoints_round_half_away_from_zero(n_cyc, expect):
+    # nu = round((2 pi / L2) * j / n) with MATLAB's round (src/initialization.m:1640): an odd
+    # wedge order with two theta points puts nu exactly on a half, which rounds up
+    k, w = cyclix_kpoints((1, 2, 1), 8.0, 2 * np.pi / n_cyc, 4.0, time_reversal=False)
+    assert k[:, 1].tolist() == expect
