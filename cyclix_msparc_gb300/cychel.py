@@ -227,11 +227,24 @@ def rot_z(theta: float) -> np.ndarray:
 
 
 def real_ylm(l: int, m: int, X, Y, Z) -> np.ndarray:
-    """Real spherical harmonics for l <= 1 (src/sphericalHarmonics.m:58-80)."""
+    """Real spherical harmonics for l <= 2 (src/sphericalHarmonics.m:58-100): the standard real
+    combinations, normalised to 1 on the unit sphere, of the direction (X, Y, Z) / r."""
     r = np.sqrt(X * X + Y * Y + Z * Z)
     if l == 0:
-        return 0.282094791773878 * np.ones_like(X)
+        return 0.5 * math.sqrt(1.0 / math.pi) * np.ones_like(X)
     if l == 1:
-        c = 0.488602511902920
+        c = math.sqrt(3.0 / (4.0 * math.pi))
         return c * {-1: Y, 0: Z, 1: X}[m] / r
-    raise ValueError("synthetic projectors use l <= 1")
+    if l == 2:
+        r2 = r * r
+        c = 0.5 * math.sqrt(15.0 / math.pi)
+        if m == -2:
+            return c * X * Y / r2
+        if m == -1:
+            return c * Y * Z / r2
+        if m == 0:
+            return 0.25 * math.sqrt(5.0 / math.pi) * (2 * Z * Z - X * X - Y * Y) / r2
+        if m == 1:
+            return c * Z * X / r2
+        return 0.25 * math.sqrt(15.0 / math.pi) * (X * X - Y * Y) / r2
+    raise ValueError("projectors with l > 2 are not supported")

@@ -1,0 +1,97 @@
+"""Pin the oracle end to end on the reference's own Cyclix decks.
+
+For each deck, the reference's input files (.inpt, .ion, .psp8) are loaded by
+``cyclix_msparc_gb300.deck`` and the oracle SCF (oracle/scf.py) runs from the atomic density
+guess.  The free energy per atom, the self and correction energy and the pseudocharge radii are
+compared with the numbers the reference printed into the deck's .out file.  The result is
+written to ``deck_pins.json`` next to this script; tests/test_decks.py checks the record and
+re-derives the fast quantities (radii, self and correction energy) from the deck files.
+
+Run from the repository root, where the reference tree is readable:
+
+    python tests/golden/pin_decks.py [deck ...]        # default: LDA_CNT
+
+Decks are paths relative to the reference project root.  A deck takes ~1 min per SCF step on
+one core (LDA_CNT: 111,320 grid points, 8 Bloch points, 15 states, degree 35).
+"""
+import json
+import os
+import re
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path[:0] = [ROOT, os.path.join(ROOT, "tests")]
+
+REFERENCE = "/root/reference/Cyclix_MS_200220"
+
+
+def out_values(out_path):
+    """Numbers the reference printed: free energy per atom, self and correction energy, radii, SCF count."""
+    txt = open(out_path).read()
+
+    def num(pat):
+        m = re.search(pat + r"\s*:\s*([-+0-9.Ee]+)", txt)
+        return float(m.group(1)) if m else None
+    radii = re.search(r"Pseudocharge radii of atom type 1\s*:\s*([0-9.]+)\s+([0-9.]+)\s+([0-9.]+)", txt)
+    nscf = re.search(r"Total number of SCF:\s*(\d+)", txt)
+    last_err = re.findall(r"^\d+\s+[-+0-9.Ee]+\s+([0-9.Ee+-]+)\s+[0-9.]+\s*$", txt, re.M)
+    return dict(free_energy_per_atom=num(r"Free energy per atom"),
+                self_and_correction=num(r"Self and correction energy"),
+                fermi_level=num(r"Fermi level"),
+                radii=[float(radii.group(i)) for i in (1, 2, 3)] if radii else None,
+                n_scf=int(nscf.group(1)) if nscf else None,
+                last_scf_error=float(last_err[-1]) if last_err else None)
+
+
+def pin(deck_rel, scf_tol=1e-6, max_scf=60):
+    from cyclix_msparc_gb300.deck import load_deck
+    from cyclix_msparc_gb300.workloads import initial_psi
+    from oracle import scf as OS
+    inpt = os.path.join(REFERENCE, deck_rel)
+    out = os.path.splitext(inpt)[0] + ".out"
+    ref = out_values(out)
+    t0 = time.time()
+    d = load_deck(inpt)
+    S = d.S
+    blocks = [(S.kptgrid[k].copy(), 0, S.Nev) for k in range(S.tnkpt)]
+    psis = [initial_psi(S.N, S.Nev, 700 + k) for k in range(S.tnkpt)]
+    hist = []
+
+    def log(it, e, err):
+        hist.append((it, float(e), float(err)))
+        print(f"  SCF {it:3d}  E = {e:.10f} Ha/atom  err = {err:.3e}  ({time.time() - t0:.0f} s)", flush=True)
+    res = OS.scf(S, psis, blocks, scf_tol=scf_tol, poisson_tol=d.poisson_tol, max_scf=max_scf, log=log)
+    E = res["Etotal"] / S.n_atm
+    # the energy when the oracle's SCF error first fell to the reference's final error
+    e_at_ref = next((e for (_, e, err) in hist if err <= ref["last_scf_error"]), None) if ref["last_scf_error"] else None
+    rec = dict(deck=deck_rel, grid=[S.Nx, S.Ny, S.Nz], n_atm=S.n_atm, n_kpt=S.tnkpt, Nev=S.Nev, npl=S.npl,
+               reference=ref,
+               oracle=dict(free_energy_per_atom=E, self_and_correction=S.E_corr - S.Eself,
+                           radii=[round(v, 6) for v in d.rb[0]], lambda_f=float(res["lambda_f"]),
+                           n_scf=res["n_scf"], scf_tol=scf_tol, energy_at_reference_error=e_at_ref,
+                           history=hist, wall_s=round(time.time() - t0, 1)),
+               diff_free_energy_per_atom=E - ref["free_energy_per_atom"],
+               diff_self_and_correction=(S.E_corr - S.Eself) - ref["self_and_correction"])
+    return rec
+
+
+def main():
+    decks = sys.argv[1:] or ["LDA_CNT/C.inpt"]
+    path = os.path.join(HERE, "deck_pins.json")
+    recs = json.load(open(path)) if os.path.exists(path) else {}
+    for dk in decks:
+        print(f"deck {dk}", flush=True)
+        recs[dk] = pin(dk)
+        print(f"  free energy per atom: oracle {recs[dk]['oracle']['free_energy_per_atom']:.10f}  "
+              f"reference {recs[dk]['reference']['free_energy_per_atom']:.10f}  "
+              f"diff {recs[dk]['diff_free_energy_per_atom']:.2e}", flush=True)
+        with open(path, "w") as f:
+            json.dump(recs, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,136 @@
+"""The deck loader against the reference's own decks and outputs (no GPU).
+
+``cyclix_msparc_gb300.deck`` reads a reference deck (.inpt, .ion, .psp8) and builds the
+pseudocharges, the self and correction energy, the pseudocharge radii and the psp8 projectors.
+Where the deck's .out was written by the committed reference code from the same input (the
+parameters it prints match the .inpt), the numbers it printed must come out again:
+
+* ``Self and correction energy`` (E_corr - Eself, src/electronicGroundState.m:95) within 1e-8 Ha
+  (the .out prints 11 significant digits);
+* ``Pseudocharge radii`` to the two decimals printed;
+* the Chebyshev degree, the number of states and the number of symmetry-reduced Bloch points.
+
+Decks whose .out came from another input or an older code version are not listed: for example
+tests/Cyclix/CNT_chiral/C.out prints FD_GRID 120 61 8 against 140 70 15 in its .inpt, and
+tests/Cyclix/CNT_ABINITmatch/C.out was written by the Sep 2019 code.
+
+The full SCF of the LDA deck is pinned by tests/golden/pin_decks.py, which writes
+tests/golden/deck_pins.json (checked below).  The reference tree is read where it exists; the
+tests skip elsewhere.
+"""
+import json
+import os
+import re
+
+import numpy as np
+import pytest
+
+REF = "/root/reference/Cyclix_MS_200220"
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+DECKS = ["LDA_CNT/C.inpt", "GGA_CNT_sg15/C.inpt", "tests/MoS2/MoS2.inpt"]
+# the reference stopped its SCF at error 8e-5 (TOL_SCF 1e-4); its last energies moved by ~3e-7 Ha/atom
+PIN_TOL_HA_PER_ATOM = 1e-5
+
+
+def _out(inpt):
+    return open(os.path.splitext(os.path.join(REF, inpt))[0] + ".out").read()
+
+
+def _need(inpt):
+    if not os.path.exists(os.path.join(REF, inpt)):
+        pytest.skip("reference decks are not present on this machine")
+
+
+@pytest.fixture(scope="module")
+def loaded():
+    from cyclix_msparc_gb300.deck import load_deck
+    cache = {}
+
+    def get(inpt):
+        if inpt not in cache:
+            cache[inpt] = load_deck(os.path.join(REF, inpt), for_scf=False)
+        return cache[inpt]
+    return get
+
+
+@pytest.mark.parametrize("inpt", DECKS)
+def test_self_and_correction_energy_and_radii(inpt, loaded):
+    _need(inpt)
+    d = loaded(inpt)
+    txt = _out(inpt)
+    ref = float(re.search(r"Self and correction energy\s*:\s*([-+0-9.Ee]+)", txt).group(1))
+    assert abs((d.S.E_corr - d.S.Eself) - ref) <= 1e-8, (d.S.E_corr - d.S.Eself, ref)
+    radii = re.findall(r"Pseudocharge radii of atom type (\d+)\s*:\s*([0-9.]+)\s+([0-9.]+)\s+([0-9.]+)", txt)
+    assert len(radii) == len(d.rb)
+    for (t, *r), rb in zip(radii, d.rb):
+        assert ["%.2f" % v for v in rb] == r, (t, rb, r)
+    # the pseudocharge integrates to minus the valence charge
+    assert abs(float(d.S.W @ d.S.b) + d.Nelectron) < 1e-4 * d.Nelectron
+
+
+@pytest.mark.parametrize("inpt", DECKS)
+def test_defaults_and_bloch_points(inpt, loaded):
+    _need(inpt)
+    d = loaded(inpt)
+    txt = _out(inpt)
+    assert int(re.search(r"CHEB_DEGREE:\s*(\d+)", txt).group(1)) == d.S.npl
+    assert int(re.search(r"NSTATES:\s*(\d+)", txt).group(1)) == d.S.Nev
+    m = re.search(r"Number of symmetry adapted k-points:\s*(\d+)", txt)
+    if m:
+        assert int(m.group(1)) == d.S.tnkpt
+        assert abs(d.S.wkpt.sum() - 1.0) < 1e-14
+
+
+def test_psp8_reader_against_the_file_text():
+    inpt = "LDA_CNT/C.inpt"
+    _need(inpt)
+    from cyclix_msparc_gb300.deck import read_psp8
+    path = os.path.join(REF, "LDA_CNT", "C.psp8")
+    p = read_psp8(path)
+    lines = open(path).read().splitlines()
+    assert p.Z == float(lines[1].split()[1]) and p.lmax == int(lines[2].split()[2]) and p.lloc == 4
+    assert p.r.shape == (int(lines[2].split()[4]),) and p.r[0] == 0.0
+    # KB energies: the numbers after the l on each projector block header
+    heads = [ln.split() for ln in lines if re.match(r"^\s{3}[0-9]\s{3,}", ln) and len(ln.split()) == 1 + p.nproj[0]]
+    assert np.allclose(p.gamma[0], [float(v) for v in heads[0][1:]])
+    assert np.allclose(p.gamma[1], [float(v) for v in heads[1][1:]])
+    # projectors divided by r, the r = 0 row copied from the next one
+    assert np.array_equal(p.proj[1][0], p.proj[1][1])
+    # the valence-density column over 4 pi (src/readPseudopot.m:68-72; only its shape matters, since
+    # the density guess is rescaled to the electron count)
+    assert p.rho_iso.max() > 0 and p.rho_iso.shape == p.r.shape
+
+
+def test_projector_layout(loaded):
+    inpt = "LDA_CNT/C.inpt"
+    _need(inpt)
+    d = loaded(inpt)
+    S = d.S
+    p = d.psps[0]
+    angnum = sum(int(p.nproj[l]) * (2 * l + 1) for l in range(p.lmax + 1))
+    for A in S.Atom:
+        assert A.angnum == angnum and A.gamma_Jl.shape == (angnum,)
+        for img in A.rcImage:
+            assert img.Chi_mat.shape == (img.rc_n_nodes, angnum)
+            assert np.all(np.isfinite(img.Chi_mat))
+            assert img.rc_pos.min() >= 1 and img.rc_pos.max() <= S.N
+    # gamma_Jl ordered (l, projector, m): l = 0 projectors once each, l = 1 three times each
+    g = S.Atom[0].gamma_Jl
+    assert np.allclose(g[:2], p.gamma[0]) and np.allclose(g[2:5], p.gamma[1][0]) and np.allclose(g[5:8], p.gamma[1][1])
+
+
+def test_scf_pin_record():
+    """The oracle SCF on the LDA deck reproduces the reference's printed free energy (the record
+    written by tests/golden/pin_decks.py; the numbers it holds are re-read from the .out here)."""
+    path = os.path.join(HERE, "golden", "deck_pins.json")
+    if not os.path.exists(path):
+        pytest.skip("no SCF pin record")
+    rec = json.load(open(path))["LDA_CNT/C.inpt"]
+    if os.path.exists(os.path.join(REF, "LDA_CNT/C.out")):
+        txt = _out("LDA_CNT/C.inpt")
+        ref = float(re.search(r"Free energy per atom\s*:\s*([-+0-9.Ee]+)", txt).group(1))
+        assert rec["reference"]["free_energy_per_atom"] == ref
+    assert rec["oracle"]["n_scf"] < 60
+    assert abs(rec["diff_free_energy_per_atom"]) <= PIN_TOL_HA_PER_ATOM, rec["diff_free_energy_per_atom"]
+
