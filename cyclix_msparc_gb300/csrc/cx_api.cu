@@ -381,6 +381,16 @@ cx_status cx_create(const cx_grid* grid, int32_t n_atm, const cx_atom* atoms, in
   if (n_atm < 0 || (n_atm > 0 && !atoms)) { g_create_err = "cx_create: atoms required"; return CX_ERR_ARG; }
   const long long Nll = (long long)G.Nx * G.Ny * G.Nz;
   if (Nll >= (1LL << 31)) { g_create_err = "cx_create: grid too large (N must fit int32)"; return CX_ERR_ARG; }
+  // projector columns per atom: the kernels hold kAngMax (l <= 1, one projector per l); a psp8
+  // atom with two projectors per l has 8 and is refused here, before any CUDA work
+  for (int J = 0; J < n_atm; ++J) {
+    const cx_atom& A = atoms[J];
+    if (A.angnum < 0 || A.angnum > kAngMax || A.n_image_rc < 0 || (A.n_image_rc > 0 && !A.rcImage) || (A.angnum > 0 && !A.gamma_Jl)) {
+      g_create_err = "cx_create: atom " + std::to_string(J) + ": angnum must be 0.." + std::to_string(kAngMax) +
+                     " (got " + std::to_string(A.angnum) + ") and rcImage/gamma_Jl given";
+      return CX_ERR_ARG;
+    }
+  }
 
   cx_handle h = new cx_handle_s();
   h->grid = G;

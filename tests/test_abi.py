@@ -92,3 +92,20 @@ def test_create_rejects_bad_spin_and_atoms(lib):
     assert lib.cx_create(C.byref(g), 2, None, 1, C.byref(h)) == 1
     assert "atoms" in lib.cx_last_error(None).decode()
     assert lib.cx_create(None, 0, None, 1, C.byref(h)) == 1
+
+
+def test_create_rejects_more_projector_columns_than_the_kernels_hold(lib):
+    # a psp8 atom with two projectors per l (l <= 1) has 8 columns; the kernels hold 4
+    import ctypes as C
+    import numpy as np
+    from cyclix_msparc_gb300 import _lib as L
+    g, keep = _grid()
+    gam = np.ones(8)
+    atoms = (L.cx_atom * 1)()
+    atoms[0].angnum = 8
+    atoms[0].n_image_rc = 0
+    atoms[0].gamma_Jl = gam.ctypes.data_as(C.POINTER(C.c_double))
+    h = C.c_void_p()
+    assert lib.cx_create(C.byref(g), 1, atoms, 1, C.byref(h)) == 1
+    msg = lib.cx_last_error(None).decode()
+    assert "angnum must be 0..4" in msg and "got 8" in msg
