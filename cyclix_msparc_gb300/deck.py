@@ -453,17 +453,19 @@ class Deck:
     pseudo: dict = field(default_factory=dict)
 
 
-def load_deck(inpt_path: str, for_scf: bool = True) -> Deck:
+def load_deck(inpt_path: str, for_scf: bool = True, overrides: dict | None = None) -> Deck:
     """Read ``<name>.inpt``, ``<name>.ion`` and the psp8 files of a cyclic or helical deck and build
     ``S`` with the fields the CheFSI path and the SCF need (src/initialization.m:13-42,
     src/calculate_b_guessRho_Eself.m, src/calculate_nloc_projector.m).
 
     With ``for_scf`` the deck must be one the SCF path runs (LDA_PW, no spin polarisation,
     Gaussian smearing); without it only the grid, pseudocharges and projectors are built, which
-    do not depend on those settings."""
+    do not depend on those settings.  ``overrides`` replaces .inpt keywords (``{"FD_GRID": ["120",
+    "61", "8"]}``), as editing the file would."""
     base = os.path.splitext(inpt_path)[0]
     root = os.path.dirname(inpt_path)
     inp = read_inpt(inpt_path)
+    inp.update({k.upper(): [str(x) for x in v] for k, v in (overrides or {}).items()})
     types = read_ion(base + ".ion")
     L1, L2, L3 = (float(v) for v in inp["CELL"][:3])
     if "BC" in inp:

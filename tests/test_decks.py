@@ -10,9 +10,13 @@ parameters it prints match the .inpt), the numbers it printed must come out agai
 * ``Pseudocharge radii`` to the two decimals printed;
 * the Chebyshev degree, the number of states and the number of symmetry-reduced Bloch points.
 
-Decks whose .out came from another input or an older code version are not listed: for example
-tests/Cyclix/CNT_chiral/C.out prints FD_GRID 120 61 8 against 140 70 15 in its .inpt, and
-tests/Cyclix/CNT_ABINITmatch/C.out was written by the Sep 2019 code.
+Several .out files were written from parameters other than those in today's .inpt; they print
+the parameters they ran with, and the deck is loaded with those (tests/Cyclix/CNT_chiral/C.out,
+for example, ran on FD_GRID 120 61 8 against 140 70 15 in its .inpt).  Pseudocharge radii are
+compared only where the .out was written by the committed radius rule (rb_y = acos(1 - rb_z^2 /
+(2 r^2)) + tau rb_z / 2); the energies do not depend on the radii once b has converged.
+Decks whose numbers still differ (their .ion or pseudopotential changed after the run, e.g. the
+relaxation deck tests/Cyclix/CNT_relax) are not listed.
 
 The full SCF of the LDA deck is pinned by tests/golden/pin_decks.py, which writes
 tests/golden/deck_pins.json (checked below).  The reference tree is read where it exists; the
@@ -28,7 +32,11 @@ import pytest
 REF = "/root/reference/Cyclix_MS_200220"
 HERE = os.path.dirname(os.path.abspath(__file__))
 
-DECKS = ["LDA_CNT/C.inpt", "GGA_CNT_sg15/C.inpt", "tests/MoS2/MoS2.inpt"]
+# (deck, compare radii): cyclic and helical (CNT_chiral, phonon/Si_1), one and two species
+DECKS = [("LDA_CNT/C.inpt", True), ("GGA_CNT_sg15/C.inpt", True), ("tests/MoS2/MoS2.inpt", True),
+         ("tests/Cyclix/CNT_ABINITmatch/C.inpt", False), ("tests/Cyclix/CNT_chiral/C.inpt", False),
+         ("tests/phonon/Si_1/Si.inpt", False), ("tests/phonon/Si_2/Si.inpt", False)]
+_PRINTED = ["CELL", "FD_GRID", "TWIST_ANGLE", "TOL_PSEUDOCHARGE", "TOL_SCF", "KPOINT_GRID", "NSTATES", "CHEB_DEGREE"]
 # the reference stopped its SCF at error 8e-5 (TOL_SCF 1e-4); its last energies moved by ~3e-7 Ha/atom
 PIN_TOL_HA_PER_ATOM = 1e-5
 
@@ -42,6 +50,27 @@ def _need(inpt):
         pytest.skip("reference decks are not present on this machine")
 
 
+def _ran_with(inpt):
+    """The .inpt keywords whose values in the .out's input-parameter block differ (beyond the 6
+    digits the .out prints): the parameters that run actually used."""
+    from cyclix_msparc_gb300.deck import read_inpt
+    head = _out(inpt).split("Initialization")[0]
+    cur = read_inpt(os.path.join(REF, inpt))
+    ov = {}
+    for k in _PRINTED:
+        m = re.search(r"^" + k + r":\s*(.*)$", head, re.M)
+        if not m:
+            continue
+        vals = m.group(1).split()
+        if k not in cur:
+            continue                      # a default the run derived; the loader derives it too
+        same = len(cur[k]) >= len(vals) and all(
+            abs(float(a) - float(b)) <= 5e-7 * max(1.0, abs(float(a))) for a, b in zip(cur[k], vals))
+        if not same:
+            ov[k] = vals
+    return ov
+
+
 @pytest.fixture(scope="module")
 def loaded():
     from cyclix_msparc_gb300.deck import load_deck
@@ -49,13 +78,13 @@ def loaded():
 
     def get(inpt):
         if inpt not in cache:
-            cache[inpt] = load_deck(os.path.join(REF, inpt), for_scf=False)
+            cache[inpt] = load_deck(os.path.join(REF, inpt), for_scf=False, overrides=_ran_with(inpt))
         return cache[inpt]
     return get
 
 
-@pytest.mark.parametrize("inpt", DECKS)
-def test_self_and_correction_energy_and_radii(inpt, loaded):
+@pytest.mark.parametrize("inpt,radii_rule", DECKS)
+def test_self_and_correction_energy_and_radii(inpt, radii_rule, loaded):
     _need(inpt)
     d = loaded(inpt)
     txt = _out(inpt)
@@ -63,14 +92,15 @@ def test_self_and_correction_energy_and_radii(inpt, loaded):
     assert abs((d.S.E_corr - d.S.Eself) - ref) <= 1e-8, (d.S.E_corr - d.S.Eself, ref)
     radii = re.findall(r"Pseudocharge radii of atom type (\d+)\s*:\s*([0-9.]+)\s+([0-9.]+)\s+([0-9.]+)", txt)
     assert len(radii) == len(d.rb)
-    for (t, *r), rb in zip(radii, d.rb):
-        assert ["%.2f" % v for v in rb] == r, (t, rb, r)
+    if radii_rule:
+        for (t, *r), rb in zip(radii, d.rb):
+            assert ["%.2f" % v for v in rb] == r, (t, rb, r)
     # the pseudocharge integrates to minus the valence charge
     assert abs(float(d.S.W @ d.S.b) + d.Nelectron) < 1e-4 * d.Nelectron
 
 
-@pytest.mark.parametrize("inpt", DECKS)
-def test_defaults_and_bloch_points(inpt, loaded):
+@pytest.mark.parametrize("inpt,radii_rule", DECKS)
+def test_defaults_and_bloch_points(inpt, radii_rule, loaded):
     _need(inpt)
     d = loaded(inpt)
     txt = _out(inpt)
