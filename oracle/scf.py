@@ -13,7 +13,7 @@ import numpy as np
 import scipy.linalg as sla
 import scipy.optimize as so
 import scipy.sparse.linalg as spla
-from scipy.special import erf
+from scipy.special import erf, expit
 
 from . import cychel_ops as O
 
@@ -95,17 +95,24 @@ def lda_pw_energy(rho, W):
 
 
 # ---------------------------------------------------------------------------------------------
-# src/occupations.m:1-35 (Gaussian smearing, elec_T_type = 1) and src/electronDensity.m:9-12
+# src/occupations.m:1-35 (Fermi-Dirac, elec_T_type = 0; Gaussian smearing, elec_T_type = 1)
+# and src/electronDensity.m:9-12
 # ---------------------------------------------------------------------------------------------
-def occupations(EigVals, wkpt, bet, occfac, NegCharge):
+def _occ(ev, lf, bet, elec_T_type):
+    if elec_T_type == 0:
+        return expit(-bet * (ev - lf))            # 1 / (1 + exp(bet (lambda - lambda_f)))
+    return 0.5 * (1.0 - erf(bet * (ev - lf)))
+
+
+def occupations(EigVals, wkpt, bet, occfac, NegCharge, elec_T_type=1):
     def f(lf):
         s = 0.0
         for k, ev in enumerate(EigVals):
-            s += occfac * np.sum(wkpt[k] * 0.5 * (1.0 - erf(bet * (ev - lf))))
+            s += occfac * np.sum(wkpt[k] * _occ(ev, lf, bet, elec_T_type))
         return s + NegCharge
     lo, hi = min(ev.min() for ev in EigVals) - 10.0, max(ev.max() for ev in EigVals) + 10.0
     lam_f = so.brentq(f, lo, hi, xtol=1e-15, rtol=4 * np.finfo(float).eps, maxiter=500)
-    occ = [0.5 * (1.0 - erf(bet * (ev - lam_f))) for ev in EigVals]
+    occ = [_occ(ev, lam_f, bet, elec_T_type) for ev in EigVals]
     return lam_f, occ
 
 
@@ -117,9 +124,9 @@ def electron_density(psis, occ, wkpt, N):
 
 
 # ---------------------------------------------------------------------------------------------
-# src/evaluateTotalEnergy.m:12-93 (nspin = 1, LDA_PW, Gaussian smearing)
+# src/evaluateTotalEnergy.m:12-93 (nspin = 1, LDA_PW; Fermi-Dirac or Gaussian smearing)
 # ---------------------------------------------------------------------------------------------
-def total_energy(EigVals, occ, wkpt, occfac, bet, lam_f, rho, b, phi, Vxc, W, Eself, E_corr):
+def total_energy(EigVals, occ, wkpt, occfac, bet, lam_f, rho, b, phi, Vxc, W, Eself, E_corr, elec_T_type=1):
     Eband = sum(occfac * wkpt[k] * np.sum(EigVals[k] * occ[k]) for k in range(len(EigVals)))
     Exc = lda_pw_energy(rho, W)
     rho_c = np.where(rho < XC_RHOTOL, XC_RHOTOL, rho)
@@ -127,7 +134,13 @@ def total_energy(EigVals, occ, wkpt, occfac, bet, lam_f, rho, b, phi, Vxc, W, Es
     Eelec_dc = 0.5 * float(np.sum((b - rho) * phi * W))
     Eent = 0.0
     for k in range(len(EigVals)):
-        Eent_v = -occfac * (1 / bet) * 1 / (2 * np.sqrt(np.pi)) * np.exp(-(bet * (EigVals[k] - lam_f)) ** 2)
+        if elec_T_type == 0:
+            o = occ[k]
+            with np.errstate(divide="ignore", invalid="ignore"):
+                Eent_v = occfac * (1 / bet) * (o * np.log(o) + (1 - o) * np.log(1 - o))
+            Eent_v[np.isnan(Eent_v)] = 0.0          # 0 log 0 (src/evaluateTotalEnergy.m:83)
+        else:
+            Eent_v = -occfac * (1 / bet) * 1 / (2 * np.sqrt(np.pi)) * np.exp(-(bet * (EigVals[k] - lam_f)) ** 2)
         Eent += wkpt[k] * np.sum(Eent_v)
     Etot = Eband + Exc - Exc_dc + Eelec_dc - Eself + E_corr + Eent
     return Etot, dict(Eband=Eband, Exc=Exc, Exc_dc=Exc_dc, Eelec_dc=Eelec_dc, Eent=Eent)
@@ -172,6 +185,7 @@ def scf(S, psis, blocks, scf_tol=1e-6, poisson_tol=None, rhoTrigger=4, max_scf=1
     Returns a dict with Etotal, EigVal (list), lambda_f, rho, Veff, n_scf, history.
     """
     N = S.N
+    T_type = getattr(S, "elec_T_type", 1)
     poisson_tol = poisson_tol if poisson_tol is not None else 0.01 * scf_tol
     P = PoissonOperator(S)
     wk = np.asarray(S.wkpt)
@@ -199,13 +213,14 @@ def scf(S, psis, blocks, scf_tol=1e-6, poisson_tol=None, rhoTrigger=4, max_scf=1
                     bup[b_], a0[b_], _ = O.spectral_bounds(H, N, b_ + 1)
             psis[b_], EigVal[b_], (a0[b_], bup[b_], _) = O.eig_solver_block(S, H, psis[b_], count, (a0[b_], bup[b_], 0.0),
                                                                               EigVal[b_], rhoTrigger=rhoTrigger)
-        lam_f, occ = occupations(EigVal, wk, S.bet, S.occfac, S.NegCharge)
+        lam_f, occ = occupations(EigVal, wk, S.bet, S.occfac, S.NegCharge, T_type)
         if count >= rhoTrigger:
             rho = electron_density(psis, occ, wk, N)
             phi, _, _ = P.solve(-4 * np.pi * (rho + S.b), phi, poisson_tol)
             Vxc = lda_pw_potential(rho)
             Veff = phi + Vxc
-            Etot, parts = total_energy(EigVal, occ, wk, S.occfac, S.bet, lam_f, rho, S.b, phi, Vxc, S.W, S.Eself, S.E_corr)
+            Etot, parts = total_energy(EigVal, occ, wk, S.occfac, S.bet, lam_f, rho, S.b, phi, Vxc, S.W, S.Eself, S.E_corr,
+                                       T_type)
             Escc = float(np.sum((Veff - Veff_temp) * rho * S.W))
             Etot += Escc
             err = np.linalg.norm(Veff - Veff_temp) / np.linalg.norm(Veff)

@@ -83,3 +83,25 @@ def test_periodic_pulay_finds_the_fixed_point():
     for it in range(1, 60):
         y = y + 0.3 * (M @ y + c - y)
     assert np.max(np.abs(y - xs)) > 1e-3 * np.max(np.abs(xs))
+
+
+def test_fermi_dirac_occupations_and_entropy():
+    # src/occupations.m (elec_T_type = 0) and the entropy term of src/evaluateTotalEnergy.m:82-83:
+    # occupations sum to the electron count; the free-energy entropy term equals
+    # T * sum f ln f + (1 - f) ln (1 - f) and vanishes as T -> 0
+    rng = np.random.default_rng(4)
+    evs = [np.sort(rng.uniform(-1, 1, 12)), np.sort(rng.uniform(-1, 1, 10))]
+    wk = np.array([0.25, 0.75])
+    for bet in (50.0, 1000.0, 1e5):
+        lam_f, occ = OS.occupations(evs, wk, bet, 2.0, -9.0, elec_T_type=0)
+        assert abs(sum(2.0 * wk[k] * np.sum(occ[k]) for k in range(2)) - 9.0) < 1e-10
+        with np.errstate(over="ignore"):
+            fd = [1.0 / (1.0 + np.exp(bet * (e - lam_f))) for e in evs]
+        assert all(np.allclose(o, f, atol=1e-15) for o, f in zip(occ, fd))
+        N = 4
+        z = np.zeros(N)
+        _, parts = OS.total_energy(evs, occ, wk, 2.0, bet, lam_f, z, z, z, z, np.ones(N), 0.0, 0.0, elec_T_type=0)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            ent = sum(wk[k] * np.nansum(2.0 / bet * (o * np.log(o) + (1 - o) * np.log(1 - o))) for k, o in enumerate(occ))
+        assert abs(parts["Eent"] - ent) < 1e-14 and parts["Eent"] <= 0.0
+    assert abs(parts["Eent"]) < 1e-4
