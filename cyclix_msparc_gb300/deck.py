@@ -458,9 +458,9 @@ def load_deck(inpt_path: str, for_scf: bool = True, overrides: dict | None = Non
     ``S`` with the fields the CheFSI path and the SCF need (src/initialization.m:13-42,
     src/calculate_b_guessRho_Eself.m, src/calculate_nloc_projector.m).
 
-    With ``for_scf`` the deck must be one the SCF path runs (LDA_PW, no spin polarisation,
-    Gaussian smearing); without it only the grid, pseudocharges and projectors are built, which
-    do not depend on those settings.  ``overrides`` replaces .inpt keywords (``{"FD_GRID": ["120",
+    With ``for_scf`` the deck must be one the SCF path runs (LDA_PW, no spin polarisation);
+    without it only the grid, pseudocharges and projectors are built, which do not depend on
+    those settings.  ``overrides`` replaces .inpt keywords (``{"FD_GRID": ["120",
     "61", "8"]}``), as editing the file would."""
     base = os.path.splitext(inpt_path)[0]
     root = os.path.dirname(inpt_path)
@@ -524,8 +524,6 @@ def load_deck(inpt_path: str, for_scf: bool = True, overrides: dict | None = Non
     if "ELEC_TEMP_TYPE" in inp:
         t = inp["ELEC_TEMP_TYPE"][0].lower()
         elec_T_type = 0 if t in ("fd", "fermi-dirac", "0") else 1
-    if for_scf and elec_T_type != 1:
-        raise ValueError("Fermi-Dirac smearing: the SCF path implements Gaussian smearing")
     if "SMEARING" in inp:
         bet = 1.0 / float(inp["SMEARING"][0])
     elif "ELEC_TEMP" in inp:

@@ -9,7 +9,8 @@ re-derives the fast quantities (radii, self and correction energy) from the deck
 
 Run from the repository root, where the reference tree is readable:
 
-    python tests/golden/pin_decks.py [deck ...]        # default: LDA_CNT
+    python tests/golden/pin_decks.py [deck ...]        # default: LDA_CNT/C.inpt
+    python tests/golden/pin_decks.py tests/Cyclix/CNT_chiral/C.inpt     # helical, Fermi-Dirac
 
 Decks are paths relative to the reference project root.  A deck takes ~1 min per SCF step on
 one core (LDA_CNT: 111,320 grid points, 8 Bloch points, 15 states, degree 35).
@@ -47,6 +48,29 @@ def out_values(out_path):
                 last_scf_error=float(last_err[-1]) if last_err else None)
 
 
+PRINTED = ["CELL", "FD_GRID", "TWIST_ANGLE", "TOL_PSEUDOCHARGE", "TOL_SCF", "KPOINT_GRID", "NSTATES", "CHEB_DEGREE"]
+
+
+def ran_with(inpt_path):
+    """The .inpt keywords whose values in the .out's input-parameter block differ (beyond the 6
+    digits the .out prints): the parameters that run actually used.  Keywords the .inpt leaves out
+    are derived defaults, which the loader derives as well."""
+    from cyclix_msparc_gb300.deck import read_inpt
+    head = open(os.path.splitext(inpt_path)[0] + ".out").read().split("Initialization")[0]
+    cur = read_inpt(inpt_path)
+    ov = {}
+    for k in PRINTED:
+        m = re.search(r"^" + k + r":\s*(.*)$", head, re.M)
+        if not m or k not in cur:
+            continue
+        vals = m.group(1).split()
+        same = len(cur[k]) >= len(vals) and all(
+            abs(float(a) - float(b)) <= 5e-7 * max(1.0, abs(float(a))) for a, b in zip(cur[k], vals))
+        if not same:
+            ov[k] = vals
+    return ov
+
+
 def pin(deck_rel, scf_tol=1e-6, max_scf=60):
     from cyclix_msparc_gb300.deck import load_deck
     from cyclix_msparc_gb300.workloads import initial_psi
@@ -55,8 +79,10 @@ def pin(deck_rel, scf_tol=1e-6, max_scf=60):
     out = os.path.splitext(inpt)[0] + ".out"
     ref = out_values(out)
     t0 = time.time()
-    d = load_deck(inpt)
+    overrides = ran_with(inpt)
+    d = load_deck(inpt, overrides=overrides)
     S = d.S
+    scf_tol = min(scf_tol, d.scf_tol)
     blocks = [(S.kptgrid[k].copy(), 0, S.Nev) for k in range(S.tnkpt)]
     psis = [initial_psi(S.N, S.Nev, 700 + k) for k in range(S.tnkpt)]
     hist = []
@@ -68,7 +94,8 @@ def pin(deck_rel, scf_tol=1e-6, max_scf=60):
     E = res["Etotal"] / S.n_atm
     # the energy when the oracle's SCF error first fell to the reference's final error
     e_at_ref = next((e for (_, e, err) in hist if err <= ref["last_scf_error"]), None) if ref["last_scf_error"] else None
-    rec = dict(deck=deck_rel, grid=[S.Nx, S.Ny, S.Nz], n_atm=S.n_atm, n_kpt=S.tnkpt, Nev=S.Nev, npl=S.npl,
+    rec = dict(deck=deck_rel, overrides=overrides, grid=[S.Nx, S.Ny, S.Nz], n_atm=S.n_atm, n_kpt=S.tnkpt, Nev=S.Nev,
+               npl=S.npl, smearing="fermi-dirac" if S.elec_T_type == 0 else "gaussian", twist=S.twist,
                reference=ref,
                oracle=dict(free_energy_per_atom=E, self_and_correction=S.E_corr - S.Eself,
                            radii=[round(v, 6) for v in d.rb[0]], lambda_f=float(res["lambda_f"]),
@@ -82,13 +109,15 @@ def pin(deck_rel, scf_tol=1e-6, max_scf=60):
 def main():
     decks = sys.argv[1:] or ["LDA_CNT/C.inpt"]
     path = os.path.join(HERE, "deck_pins.json")
-    recs = json.load(open(path)) if os.path.exists(path) else {}
     for dk in decks:
         print(f"deck {dk}", flush=True)
-        recs[dk] = pin(dk)
-        print(f"  free energy per atom: oracle {recs[dk]['oracle']['free_energy_per_atom']:.10f}  "
-              f"reference {recs[dk]['reference']['free_energy_per_atom']:.10f}  "
-              f"diff {recs[dk]['diff_free_energy_per_atom']:.2e}", flush=True)
+        rec = pin(dk)
+        print(f"  free energy per atom: oracle {rec['oracle']['free_energy_per_atom']:.10f}  "
+              f"reference {rec['reference']['free_energy_per_atom']:.10f}  "
+              f"diff {rec['diff_free_energy_per_atom']:.2e}", flush=True)
+        # merge with the records other runs wrote meanwhile
+        recs = json.load(open(path)) if os.path.exists(path) else {}
+        recs[dk] = rec
         with open(path, "w") as f:
             json.dump(recs, f, indent=1)
 

@@ -36,7 +36,6 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 DECKS = [("LDA_CNT/C.inpt", True), ("GGA_CNT_sg15/C.inpt", True), ("tests/MoS2/MoS2.inpt", True),
          ("tests/Cyclix/CNT_ABINITmatch/C.inpt", False), ("tests/Cyclix/CNT_chiral/C.inpt", False),
          ("tests/phonon/Si_1/Si.inpt", False), ("tests/phonon/Si_2/Si.inpt", False)]
-_PRINTED = ["CELL", "FD_GRID", "TWIST_ANGLE", "TOL_PSEUDOCHARGE", "TOL_SCF", "KPOINT_GRID", "NSTATES", "CHEB_DEGREE"]
 # the reference stopped its SCF at error 8e-5 (TOL_SCF 1e-4); its last energies moved by ~3e-7 Ha/atom
 PIN_TOL_HA_PER_ATOM = 1e-5
 
@@ -51,24 +50,8 @@ def _need(inpt):
 
 
 def _ran_with(inpt):
-    """The .inpt keywords whose values in the .out's input-parameter block differ (beyond the 6
-    digits the .out prints): the parameters that run actually used."""
-    from cyclix_msparc_gb300.deck import read_inpt
-    head = _out(inpt).split("Initialization")[0]
-    cur = read_inpt(os.path.join(REF, inpt))
-    ov = {}
-    for k in _PRINTED:
-        m = re.search(r"^" + k + r":\s*(.*)$", head, re.M)
-        if not m:
-            continue
-        vals = m.group(1).split()
-        if k not in cur:
-            continue                      # a default the run derived; the loader derives it too
-        same = len(cur[k]) >= len(vals) and all(
-            abs(float(a) - float(b)) <= 5e-7 * max(1.0, abs(float(a))) for a, b in zip(cur[k], vals))
-        if not same:
-            ov[k] = vals
-    return ov
+    from golden.pin_decks import ran_with
+    return ran_with(os.path.join(REF, inpt))
 
 
 @pytest.fixture(scope="module")
