@@ -91,15 +91,19 @@ def poisson_case() -> dict:
     return dict(phi=phi, relres=relres, iters=it)
 
 
-def scf_small(name: str = "scf-small-24x12x20-12at-2k-ns40") -> dict:
-    """The oracle SCF (src/scf.m) on a small cell, tol 1e-6, psi = initial_psi(N, Ns, 7 + b)."""
+def scf_small(name: str = "scf-small-24x12x20-12at-2k-ns40", fermi_dirac: bool = False) -> dict:
+    """The oracle SCF (src/scf.m) on a small cell, tol 1e-6, psi = initial_psi(N, Ns, 7 + b);
+    Gaussian smearing, or Fermi-Dirac at the same smearing width."""
     wl = WORKLOADS[name]
     S = make_system(wl)
+    if fermi_dirac:
+        S.elec_T_type = 0
     bl = block_layout(wl, S)
     psis = [initial_psi(S.N, n, 7 + i) for i, (_, _, n) in enumerate(bl)]
     from oracle.scf import scf
     r = scf(S, psis, bl, scf_tol=1e-6)
-    return dict(workload=wl.name, scf_tol=1e-6, n_atm=S.n_atm, Etotal=r["Etotal"], E_per_atom=r["Etotal"] / S.n_atm,
+    return dict(workload=wl.name, smearing="fermi-dirac" if fermi_dirac else "gaussian", scf_tol=1e-6, n_atm=S.n_atm,
+                Etotal=r["Etotal"], E_per_atom=r["Etotal"] / S.n_atm,
                 lambda_f=r["lambda_f"], n_scf=r["n_scf"], history=[list(h) for h in r["history"]],
                 EigVal=[ev.tolist() for ev in r["EigVal"]])
 
@@ -114,6 +118,8 @@ def write_all(which=None):
         "scf_small": lambda: (HERE / "scf_small.json").write_text(json.dumps(scf_small(), indent=1)),
         "scf_small_helical": lambda: (HERE / "scf_small_helical.json").write_text(
             json.dumps(scf_small("scf-small-helical-24x12x16-8at-2k-ns28"), indent=1)),
+        "scf_small_fd": lambda: (HERE / "scf_small_fd.json").write_text(
+            json.dumps(scf_small(fermi_dirac=True), indent=1)),
     }
     for k, fn in jobs.items():
         if which is None or k in which:

@@ -42,10 +42,11 @@ def test_poisson_golden():
 
 @pytest.mark.slow
 @pytest.mark.parametrize("name,fixture", [("scf-small-24x12x20-12at-2k-ns40", "scf_small.json"),
-                                          ("scf-small-helical-24x12x16-8at-2k-ns28", "scf_small_helical.json")])
+                                          ("scf-small-helical-24x12x16-8at-2k-ns28", "scf_small_helical.json"),
+                                          ("scf-small-24x12x20-12at-2k-ns40", "scf_small_fd.json")])
 def test_scf_golden(name, fixture):
     ref = json.loads((GOLD / fixture).read_text())
-    out = G.scf_small(name)
+    out = G.scf_small(name, fermi_dirac=ref.get("smearing") == "fermi-dirac")
     assert out["n_scf"] == ref["n_scf"]
     assert abs(out["E_per_atom"] - ref["E_per_atom"]) < 1e-10
     for a, b in zip(out["EigVal"], ref["EigVal"]):

@@ -1,5 +1,6 @@
 """GPU SCF (cx_scf, src/scf.m) against the oracle SCF fixtures: the cyclic 24 x 12 x 20 12-atom cell
-and the helical (twist 0.05 rad/bohr) 24 x 12 x 16 8-atom cell.
+(Gaussian and Fermi-Dirac smearing, src/occupations.m) and the helical (twist 0.05 rad/bohr)
+24 x 12 x 16 8-atom cell.
 
 Tolerances:
   * complex128: total energy within 1e-7 Ha/atom of the oracle, Fermi level within 1e-5 Ha and
@@ -22,15 +23,18 @@ GOLD = Path(__file__).resolve().parent / "golden"
 
 
 CASES = [("scf-small-24x12x20-12at-2k-ns40", "scf_small.json", 24),
-         ("scf-small-helical-24x12x16-8at-2k-ns28", "scf_small_helical.json", 16)]
+         ("scf-small-helical-24x12x16-8at-2k-ns28", "scf_small_helical.json", 16),
+         ("scf-small-24x12x20-12at-2k-ns40", "scf_small_fd.json", 24)]
 
 
-@pytest.fixture(scope="module", params=CASES, ids=[c[0] for c in CASES])
+@pytest.fixture(scope="module", params=CASES, ids=[c[1].split(".")[0] for c in CASES])
 def scf_system(request):
     name, fixture, nocc = request.param
     wl = WORKLOADS[name]
     S = make_system(wl)
     ref = json.loads((GOLD / fixture).read_text())
+    if ref.get("smearing") == "fermi-dirac":
+        S.elec_T_type = 0
     return wl, S, block_layout(wl, S), ref, nocc
 
 
