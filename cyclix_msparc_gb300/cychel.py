@@ -130,6 +130,29 @@ class CyclixS:
         return self.xin + self.L1
 
 
+def split_projector_columns(atoms: list, width: int = 4) -> tuple[list, list]:
+    """Atoms whose projector columns fit ``width``.
+
+    The Kleinman-Bylander term sum_J sum_c gamma_Jc |chi_Jc><chi_Jc| (src/h_nonlocal_vector_mult.m:
+    24-43) is a sum over the columns c of each atom with a diagonal gamma, so an atom with more
+    columns (a psp8 atom with two projectors per l has 8, one with l <= 2 has 18) equals several
+    atoms at the same position and images holding consecutive slices of its columns.  Returns the
+    list of such atoms and, for each, the index of the atom it came from.
+    """
+    out, origin = [], []
+    for J, A in enumerate(atoms):
+        if A.angnum <= width:
+            out.append(A)
+            origin.append(J)
+            continue
+        for c0 in range(0, A.angnum, width):
+            c1 = min(c0 + width, A.angnum)
+            imgs = [RcImage(img.coordinates, img.rc_pos, np.ascontiguousarray(img.Chi_mat[:, c0:c1])) for img in A.rcImage]
+            out.append(AtomNL(c1 - c0, np.asarray(A.gamma_Jl[c0:c1]), imgs))
+            origin.append(J)
+    return out, origin
+
+
 def cell_type(helical: bool) -> tuple[int, int, int, int]:
     """(cell_typ, BCx, BCy, BCz) for ``BC: D C P`` (cyclic) or ``D C H`` (cyclic+helical).
 

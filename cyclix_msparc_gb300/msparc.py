@@ -21,6 +21,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import CxError, check, cptr, dptr
+from .cychel import split_projector_columns
 
 __all__ = ["CyclixGPU", "attach", "h_nonlocal_vector_mult", "chebyshev_filter", "eigSolver", "poissonSolve", "scf", "CxError"]
 
@@ -59,8 +60,11 @@ class CyclixGPU:
         g = _lib.cx_grid(Nx=S.Nx, Ny=S.Ny, Nz=S.Nz, FDn=S.FDn, cell_typ=S.cell_typ, BCx=S.BCx, BCy=S.BCy, BCz=S.BCz,
                          dx=S.dx, dy=S.dy, dz=S.dz, xin=S.xin, twist=S.twist, L1=S.L1, L2=S.L2, L3=S.L3,
                          w1=darr(S.w1), w2=darr(S.w2), W=darr(S.W))
-        atoms = (_lib.cx_atom * max(1, len(S.Atom)))()
-        for J, A in enumerate(S.Atom):
+        # the library's projector kernels hold 4 columns per atom: psp8 atoms with more are passed
+        # as several atoms at the same position (the same operator, see split_projector_columns)
+        nl_atoms, origin = split_projector_columns(S.Atom, 4)
+        atoms = (_lib.cx_atom * max(1, len(nl_atoms)))()
+        for J, A in enumerate(nl_atoms):
             imgs = (_lib.cx_rc_image * max(1, A.n_image_rc))()
             keep.append(imgs)
             for k, img in enumerate(A.rcImage):
@@ -76,10 +80,10 @@ class CyclixGPU:
             atoms[J].n_image_rc = int(A.n_image_rc)
             atoms[J].gamma_Jl = darr(A.gamma_Jl)
             for d in range(3):
-                atoms[J].position[d] = float(S.Atoms[J, d])
+                atoms[J].position[d] = float(S.Atoms[origin[J], d])
             atoms[J].rcImage = C.cast(imgs, C.POINTER(_lib.cx_rc_image))
         h = C.c_void_p()
-        st = self.lib.cx_create(C.byref(g), len(S.Atom), atoms, int(S.nspin), C.byref(h))
+        st = self.lib.cx_create(C.byref(g), len(nl_atoms), atoms, int(S.nspin), C.byref(h))
         if st != _lib.CX_OK:
             raise CxError(st, self.lib.cx_last_error(None).decode())
         self.h = h

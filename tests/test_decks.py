@@ -147,3 +147,31 @@ def test_scf_pin_record():
     assert rec["oracle"]["n_scf"] < 60
     assert abs(rec["diff_free_energy_per_atom"]) <= PIN_TOL_HA_PER_ATOM, rec["diff_free_energy_per_atom"]
 
+
+
+def test_split_projector_columns_is_the_same_operator(loaded):
+    """psp8 atoms with 8 projector columns go to the GPU library as two 4-column atoms at the same
+    position (the kernels hold 4); the KB term is a sum over columns, so H is unchanged (checked
+    with the oracle H at a Bloch point with phases, nu = 2)."""
+    inpt = "LDA_CNT/C.inpt"
+    _need(inpt)
+    import copy
+    from cyclix_msparc_gb300.cychel import split_projector_columns
+    from oracle import cychel_ops as O
+    d = loaded(inpt)
+    S = d.S
+    atoms, origin = split_projector_columns(S.Atom, 4)
+    assert len(atoms) == 2 * len(S.Atom) and all(A.angnum == 4 for A in atoms)
+    assert origin == [J for J in range(len(S.Atom)) for _ in range(2)]
+    S2 = copy.copy(S)
+    S2.Atom, S2.Atoms = atoms, S.Atoms[origin]
+    rng = np.random.default_rng(3)
+    X = rng.standard_normal((S.N, 3)) + 1j * rng.standard_normal((S.N, 3))
+    V = S.rho_at
+    for k in (S.kptgrid[0], S.kptgrid[1]):
+        Y1 = O.Hamiltonian(S, k, V)(X)
+        Y2 = O.Hamiltonian(S2, k, V)(X)
+        assert np.max(np.abs(Y1 - Y2)) <= 1e-13 * np.max(np.abs(Y1))
+    # atoms that fit are passed through unchanged
+    same, org = split_projector_columns(atoms, 4)
+    assert same == atoms and org == list(range(len(atoms)))
