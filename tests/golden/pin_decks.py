@@ -12,8 +12,10 @@ Run from the repository root, where the reference tree is readable:
     python tests/golden/pin_decks.py [deck ...]        # default: LDA_CNT/C.inpt
     python tests/golden/pin_decks.py tests/Cyclix/CNT_chiral/C.inpt     # helical, Fermi-Dirac
 
-Decks are paths relative to the reference project root.  A deck takes ~1 min per SCF step on
-one core (LDA_CNT: 111,320 grid points, 8 Bloch points, 15 states, degree 35).
+Decks are paths relative to the reference project root (``--root DIR`` reads a copy of the deck
+files elsewhere).  A deck takes ~1 min per SCF step on one core (LDA_CNT: 111,320 grid points,
+8 Bloch points, 15 states, degree 35).  ``--gpu fp64|mixed`` runs the same SCF through the GPU
+library (``CyclixGPU.scf``) instead of the oracle and records it under ``<deck>@gpu-<prec>``.
 """
 import json
 import os
@@ -71,11 +73,24 @@ def ran_with(inpt_path):
     return ov
 
 
-def pin(deck_rel, scf_tol=1e-6, max_scf=60):
+def _gpu_scf(S, blocks, psis, prec, scf_tol, poisson_tol, max_scf, log):
+    from cyclix_msparc_gb300.msparc import CyclixGPU
+    g = CyclixGPU(S, blocks, prec)
+    try:
+        for b, p in enumerate(psis):
+            g.set_psi(b, p)
+        res, EV, rho, V, hist = g.scf(S, scf_tol=scf_tol, poisson_tol=poisson_tol, max_scf=max_scf)
+    finally:
+        g.close()
+    for it, (e, err) in enumerate(hist, 1):
+        log(it, e, err)
+    return dict(Etotal=res.Etotal, lambda_f=res.lambda_f, n_scf=res.n_scf)
+
+
+def pin(deck_rel, scf_tol=1e-6, max_scf=60, root=REFERENCE, gpu=None):
     from cyclix_msparc_gb300.deck import load_deck
     from cyclix_msparc_gb300.workloads import initial_psi
-    from oracle import scf as OS
-    inpt = os.path.join(REFERENCE, deck_rel)
+    inpt = os.path.join(root, deck_rel)
     out = os.path.splitext(inpt)[0] + ".out"
     ref = out_values(out)
     t0 = time.time()
@@ -90,11 +105,15 @@ def pin(deck_rel, scf_tol=1e-6, max_scf=60):
     def log(it, e, err):
         hist.append((it, float(e), float(err)))
         print(f"  SCF {it:3d}  E = {e:.10f} Ha/atom  err = {err:.3e}  ({time.time() - t0:.0f} s)", flush=True)
-    res = OS.scf(S, psis, blocks, scf_tol=scf_tol, poisson_tol=d.poisson_tol, max_scf=max_scf, log=log)
+    if gpu:
+        res = _gpu_scf(S, blocks, psis, gpu, scf_tol, d.poisson_tol, max_scf, log)
+    else:
+        from oracle import scf as OS
+        res = OS.scf(S, psis, blocks, scf_tol=scf_tol, poisson_tol=d.poisson_tol, max_scf=max_scf, log=log)
     E = res["Etotal"] / S.n_atm
     # the energy when the oracle's SCF error first fell to the reference's final error
     e_at_ref = next((e for (_, e, err) in hist if err <= ref["last_scf_error"]), None) if ref["last_scf_error"] else None
-    rec = dict(deck=deck_rel, overrides=overrides, grid=[S.Nx, S.Ny, S.Nz], n_atm=S.n_atm, n_kpt=S.tnkpt, Nev=S.Nev,
+    rec = dict(deck=deck_rel, solver=f"gpu-{gpu}" if gpu else "oracle", overrides=overrides, grid=[S.Nx, S.Ny, S.Nz], n_atm=S.n_atm, n_kpt=S.tnkpt, Nev=S.Nev,
                npl=S.npl, smearing="fermi-dirac" if S.elec_T_type == 0 else "gaussian", twist=S.twist,
                reference=ref,
                oracle=dict(free_energy_per_atom=E, self_and_correction=S.E_corr - S.Eself,
@@ -107,17 +126,23 @@ def pin(deck_rel, scf_tol=1e-6, max_scf=60):
 
 
 def main():
-    decks = sys.argv[1:] or ["LDA_CNT/C.inpt"]
-    path = os.path.join(HERE, "deck_pins.json")
-    for dk in decks:
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("decks", nargs="*", default=["LDA_CNT/C.inpt"])
+    ap.add_argument("--root", default=REFERENCE, help="directory holding the decks (reference project root)")
+    ap.add_argument("--gpu", choices=["fp64", "mixed"], help="run the SCF through the GPU library")
+    ap.add_argument("--out", default=os.path.join(HERE, "deck_pins.json"))
+    args = ap.parse_args()
+    path = args.out
+    for dk in args.decks:
         print(f"deck {dk}", flush=True)
-        rec = pin(dk)
+        rec = pin(dk, root=args.root, gpu=args.gpu)
         print(f"  free energy per atom: oracle {rec['oracle']['free_energy_per_atom']:.10f}  "
               f"reference {rec['reference']['free_energy_per_atom']:.10f}  "
               f"diff {rec['diff_free_energy_per_atom']:.2e}", flush=True)
         # merge with the records other runs wrote meanwhile
         recs = json.load(open(path)) if os.path.exists(path) else {}
-        recs[dk] = rec
+        recs[dk + (f"@gpu-{args.gpu}" if args.gpu else "")] = rec
         with open(path, "w") as f:
             json.dump(recs, f, indent=1)
 
