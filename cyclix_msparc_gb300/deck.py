@@ -482,8 +482,8 @@ def load_deck(inpt_path: str, for_scf: bool = True, overrides: dict | None = Non
     if cell_typ == 3:
         twist = 0.0
     xc = inp.get("EXCHANGE_CORRELATION", ["LDA_PW"])[0]
-    if for_scf and xc != "LDA_PW":
-        raise ValueError(f"exchange-correlation {xc}: the SCF path implements LDA_PW")
+    if for_scf and xc not in ("LDA_PW", "LDA_PZ"):
+        raise ValueError(f"exchange-correlation {xc}: the SCF paths implement LDA_PW (and the oracle LDA_PZ)")
     if for_scf and "SPIN_TYP" in inp and int(inp["SPIN_TYP"][0]) != 0:
         raise ValueError("spin-polarised decks are not supported by the SCF path")
     Nx0, Ny0, Nz0 = (int(v) for v in inp["FD_GRID"][:3])
@@ -539,5 +539,5 @@ def load_deck(inpt_path: str, for_scf: bool = True, overrides: dict | None = Non
     S.b, S.rho_at, S.NegCharge = pc["b"], pc["rho_at"], pc["NegCharge"]
     S.Eself, S.E_corr = pc["Eself"], pc["E_corr"]
     S.bet, S.elec_T_type, S.occfac, S.n_atm = bet, elec_T_type, 2.0, int(Atoms.shape[0])
-    S.extra.update(deck=os.path.basename(base), atom_type=atom_type, xvac=xvac)
+    S.extra.update(deck=os.path.basename(base), atom_type=atom_type, xvac=xvac, xc=xc)
     return Deck(S, inp, types, psps, rbs, scf_tol, poisson_tol, Nelectron, pc)

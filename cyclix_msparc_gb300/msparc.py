@@ -167,6 +167,9 @@ class CyclixGPU:
     def scf(self, S, scf_tol=1e-6, poisson_tol=-1.0, max_scf=100, min_scf=3, rhoTrigger=4, maxit_poisson=1000,
             mixing_param=0.3, refine=None):
         """Full SCF on the device-resident psi (cx_scf); returns (result, EigVal packed, rho, Veff, history)."""
+        xc = S.extra.get("xc", "LDA_PW") if hasattr(S, "extra") else "LDA_PW"
+        if xc != "LDA_PW":
+            raise CxError(_lib.CX_ERR_ARG, f"cx_scf implements LDA_PW, not {xc}")
         wk = np.ascontiguousarray([S.wkpt[i % S.tnkpt] for i in range(len(self.blocks))], dtype=np.float64)
         b = np.ascontiguousarray(S.b, dtype=np.float64)
         rho0 = np.ascontiguousarray(S.rho_at, dtype=np.float64)

@@ -1,7 +1,7 @@
 """Oracle restatement of the SCF bookkeeping around the CheFSI path.
 
 Test infrastructure only (see ``oracle/__init__.py``).  Paths relative to the reference project
-root ``Cyclix_MS_200220/``.  Covers the non-spin LDA_PW potential-mixing SCF of src/scf.m with the
+root ``Cyclix_MS_200220/``.  Covers the non-spin LDA (PW or PZ) potential-mixing SCF of src/scf.m with the
 reference defaults (MixingVariable = 1, MixingPrecond = 0, PulayFrequency = 1, MixingHistory = 7,
 MixingParameter = 0.3, rhoTrigger = 4, MINIT_SCF = 3; src/initialization.m:1004-1040).
 """
@@ -95,6 +95,56 @@ def lda_pw_energy(rho, W):
 
 
 # ---------------------------------------------------------------------------------------------
+# LDA_PZ: Slater exchange and the Perdew-Zunger (1981) parametrisation of the Ceperley-Alder
+# correlation, unpolarised.  The reference's potential comes from compiled libxc (functional ids
+# 1 and 9, src/exchangeCorrelationPotential.m:109-130), restated here from the published
+# formulas; its energy is src/evaluateTotalEnergy.m:44-60.
+# ---------------------------------------------------------------------------------------------
+PZ = dict(A=0.0311, B=-0.048, C=0.002, D=-0.0116, gamma=-0.1423, beta1=1.0529, beta2=0.3334)
+
+
+def _pz_corr(rho):
+    """(eps_c, v_c) of Perdew-Zunger: rs >= 1 Pade form, rs < 1 logarithmic form."""
+    rs = (0.75 / (np.pi * rho)) ** (1 / 3)
+    A, B, C, D = PZ["A"], PZ["B"], PZ["C"], PZ["D"]
+    g, b1, b2 = PZ["gamma"], PZ["beta1"], PZ["beta2"]
+    eps = np.empty_like(rs)
+    v = np.empty_like(rs)
+    hi = rs >= 1.0
+    sq = np.sqrt(rs[hi])
+    den = 1.0 + b1 * sq + b2 * rs[hi]
+    eps[hi] = g / den
+    v[hi] = eps[hi] * (1.0 + (7.0 / 6.0) * b1 * sq + (4.0 / 3.0) * b2 * rs[hi]) / den
+    lo = ~hi
+    r = rs[lo]
+    lr = np.log(r)
+    eps[lo] = A * lr + B + C * r * lr + D * r
+    v[lo] = A * lr + (B - A / 3.0) + (2.0 / 3.0) * C * r * lr + (2.0 * D - C) / 3.0 * r
+    return eps, v
+
+
+def lda_pz_potential(rho):
+    rho = np.where(rho < XC_RHOTOL, XC_RHOTOL, rho)
+    vx = -((3.0 / np.pi) * rho) ** (1 / 3)          # d(rho eps_x)/d rho, eps_x = -(3/4)(3 rho/pi)^(1/3)
+    return vx + _pz_corr(rho)[1]
+
+
+def lda_pz_energy(rho, W):
+    rho = np.where(rho < XC_RHOTOL, XC_RHOTOL, rho)
+    C2 = 0.73855876638202                         # (3/4)(3/pi)^(1/3)
+    return float(np.sum(_pz_corr(rho)[0] * rho * W) - C2 * np.sum(rho ** (4 / 3) * W))
+
+
+def xc_functions(name):
+    """(potential, energy) of an LDA functional by the reference's EXCHANGE_CORRELATION name."""
+    if name == "LDA_PW":
+        return lda_pw_potential, lda_pw_energy
+    if name == "LDA_PZ":
+        return lda_pz_potential, lda_pz_energy
+    raise ValueError(f"exchange-correlation {name}: the oracle implements LDA_PW and LDA_PZ")
+
+
+# ---------------------------------------------------------------------------------------------
 # src/occupations.m:1-35 (Fermi-Dirac, elec_T_type = 0; Gaussian smearing, elec_T_type = 1)
 # and src/electronDensity.m:9-12
 # ---------------------------------------------------------------------------------------------
@@ -126,9 +176,10 @@ def electron_density(psis, occ, wkpt, N):
 # ---------------------------------------------------------------------------------------------
 # src/evaluateTotalEnergy.m:12-93 (nspin = 1, LDA_PW; Fermi-Dirac or Gaussian smearing)
 # ---------------------------------------------------------------------------------------------
-def total_energy(EigVals, occ, wkpt, occfac, bet, lam_f, rho, b, phi, Vxc, W, Eself, E_corr, elec_T_type=1):
+def total_energy(EigVals, occ, wkpt, occfac, bet, lam_f, rho, b, phi, Vxc, W, Eself, E_corr, elec_T_type=1,
+                 exc_energy=None):
     Eband = sum(occfac * wkpt[k] * np.sum(EigVals[k] * occ[k]) for k in range(len(EigVals)))
-    Exc = lda_pw_energy(rho, W)
+    Exc = (exc_energy or lda_pw_energy)(rho, W)
     rho_c = np.where(rho < XC_RHOTOL, XC_RHOTOL, rho)
     Exc_dc = float(np.sum(Vxc * rho_c * W))
     Eelec_dc = 0.5 * float(np.sum((b - rho) * phi * W))
@@ -186,12 +237,13 @@ def scf(S, psis, blocks, scf_tol=1e-6, poisson_tol=None, rhoTrigger=4, max_scf=1
     """
     N = S.N
     T_type = getattr(S, "elec_T_type", 1)
+    vxc_fn, exc_fn = xc_functions(S.extra.get("xc", "LDA_PW"))
     poisson_tol = poisson_tol if poisson_tol is not None else 0.01 * scf_tol
     P = PoissonOperator(S)
     wk = np.asarray(S.wkpt)
     rho = S.rho_at.copy()
     phi, _, _ = P.solve(-4 * np.pi * (rho + S.b), None, poisson_tol)
-    Vxc = lda_pw_potential(rho)
+    Vxc = vxc_fn(rho)
     Veff = phi + Vxc
     mixer = PeriodicPulay(N)
     Veff_temp = Veff.copy()
@@ -217,10 +269,10 @@ def scf(S, psis, blocks, scf_tol=1e-6, poisson_tol=None, rhoTrigger=4, max_scf=1
         if count >= rhoTrigger:
             rho = electron_density(psis, occ, wk, N)
             phi, _, _ = P.solve(-4 * np.pi * (rho + S.b), phi, poisson_tol)
-            Vxc = lda_pw_potential(rho)
+            Vxc = vxc_fn(rho)
             Veff = phi + Vxc
             Etot, parts = total_energy(EigVal, occ, wk, S.occfac, S.bet, lam_f, rho, S.b, phi, Vxc, S.W, S.Eself, S.E_corr,
-                                       T_type)
+                                       T_type, exc_fn)
             Escc = float(np.sum((Veff - Veff_temp) * rho * S.W))
             Etot += Escc
             err = np.linalg.norm(Veff - Veff_temp) / np.linalg.norm(Veff)

@@ -105,3 +105,25 @@ def test_fermi_dirac_occupations_and_entropy():
             ent = sum(wk[k] * np.nansum(2.0 / bet * (o * np.log(o) + (1 - o) * np.log(1 - o))) for k, o in enumerate(occ))
         assert abs(parts["Eent"] - ent) < 1e-14 and parts["Eent"] <= 0.0
     assert abs(parts["Eent"]) < 1e-4
+
+
+@pytest.mark.parametrize("rho", [1e-4, 3e-3, 0.05, 0.7, 4.0])
+def test_lda_pz_potential_is_the_energy_derivative(rho):
+    # both branches of the Perdew-Zunger fit (rs >= 1 and rs < 1 at rho > 0.24) and their
+    # potentials: V_xc = d(rho eps_xc)/d rho
+    W = np.ones(1)
+    h = 1e-6 * rho
+    e = lambda r: OS.lda_pz_energy(np.array([r]), W)
+    dnum = (e(rho + h) - e(rho - h)) / (2 * h)
+    v = OS.lda_pz_potential(np.array([rho]))[0]
+    assert abs(v - dnum) < 1e-6 * max(1.0, abs(v))
+
+
+def test_lda_pz_close_to_pw():
+    # two fits of the same Ceperley-Alder data: within a few mHa per electron over metallic densities
+    rho = np.geomspace(1e-3, 1.0, 20)
+    W = np.ones(1)
+    for r in rho:
+        a = OS.lda_pz_energy(np.array([r]), W) / r
+        b = OS.lda_pw_energy(np.array([r]), W) / r
+        assert abs(a - b) < 3e-3
