@@ -467,6 +467,9 @@ def load_deck(inpt_path: str, for_scf: bool = True, overrides: dict | None = Non
     inp = read_inpt(inpt_path)
     inp.update({k.upper(): [str(x) for x in v] for k, v in (overrides or {}).items()})
     types = read_ion(base + ".ion")
+    if "PSEUDO_POT" in inp:                      # one file per atom type, in .ion order
+        for T, f in zip(types, inp["PSEUDO_POT"]):
+            T.psp_file = f
     L1, L2, L3 = (float(v) for v in inp["CELL"][:3])
     if "BC" in inp:
         bc = [c.upper() for c in inp["BC"][:3]]

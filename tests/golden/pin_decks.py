@@ -55,12 +55,19 @@ PRINTED = ["CELL", "FD_GRID", "TWIST_ANGLE", "TOL_PSEUDOCHARGE", "TOL_SCF", "KPO
 
 def ran_with(inpt_path):
     """The .inpt keywords whose values in the .out's input-parameter block differ (beyond the 6
-    digits the .out prints): the parameters that run actually used.  Keywords the .inpt leaves out
-    are derived defaults, which the loader derives as well."""
-    from cyclix_msparc_gb300.deck import read_inpt
-    head = open(os.path.splitext(inpt_path)[0] + ".out").read().split("Initialization")[0]
+    digits the .out prints), and the pseudopotential files the run read where the .ion now names
+    others: the parameters that run actually used.  Keywords the .inpt leaves out are derived
+    defaults, which the loader derives as well."""
+    from cyclix_msparc_gb300.deck import read_inpt, read_ion
+    txt = open(os.path.splitext(inpt_path)[0] + ".out").read()
+    head = txt.split("Initialization")[0]
     cur = read_inpt(inpt_path)
     ov = {}
+    # the pseudopotential files the run read (one line per atom type)
+    used = re.findall(r"^Pseudopotential\s*:\s*(\S+)", txt, re.M)
+    files = [T.psp_file for T in read_ion(os.path.splitext(inpt_path)[0] + ".ion")]
+    if used and len(used) == len(files) and [os.path.basename(u) for u in used] != [os.path.basename(f) for f in files]:
+        ov["PSEUDO_POT"] = [os.path.basename(u) for u in used]
     for k in PRINTED:
         m = re.search(r"^" + k + r":\s*(.*)$", head, re.M)
         if not m or k not in cur:
