@@ -485,8 +485,8 @@ def load_deck(inpt_path: str, for_scf: bool = True, overrides: dict | None = Non
     if cell_typ == 3:
         twist = 0.0
     xc = inp.get("EXCHANGE_CORRELATION", ["LDA_PW"])[0]
-    if for_scf and xc not in ("LDA_PW", "LDA_PZ"):
-        raise ValueError(f"exchange-correlation {xc}: the SCF paths implement LDA_PW (and the oracle LDA_PZ)")
+    if for_scf and xc not in ("LDA_PW", "LDA_PZ", "GGA_PBE"):
+        raise ValueError(f"exchange-correlation {xc}: the SCF paths implement LDA_PW (and the oracle LDA_PZ, GGA_PBE)")
     if for_scf and "SPIN_TYP" in inp and int(inp["SPIN_TYP"][0]) != 0:
         raise ValueError("spin-polarised decks are not supported by the SCF path")
     Nx0, Ny0, Nz0 = (int(v) for v in inp["FD_GRID"][:3])

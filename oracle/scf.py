@@ -1,7 +1,7 @@
 """Oracle restatement of the SCF bookkeeping around the CheFSI path.
 
 Test infrastructure only (see ``oracle/__init__.py``).  Paths relative to the reference project
-root ``Cyclix_MS_200220/``.  Covers the non-spin LDA (PW or PZ) potential-mixing SCF of src/scf.m with the
+root ``Cyclix_MS_200220/``.  Covers the non-spin LDA (PW or PZ) and GGA_PBE potential-mixing SCF of src/scf.m with the
 reference defaults (MixingVariable = 1, MixingPrecond = 0, PulayFrequency = 1, MixingHistory = 7,
 MixingParameter = 0.3, rhoTrigger = 4, MINIT_SCF = 3; src/initialization.m:1004-1040).
 """
@@ -12,6 +12,7 @@ import math
 import numpy as np
 import scipy.linalg as sla
 import scipy.optimize as so
+import scipy.sparse as sp
 import scipy.sparse.linalg as spla
 from scipy.special import erf, expit
 
@@ -135,13 +136,107 @@ def lda_pz_energy(rho, W):
     return float(np.sum(_pz_corr(rho)[0] * rho * W) - C2 * np.sum(rho ** (4 / 3) * W))
 
 
-def xc_functions(name):
-    """(potential, energy) of an LDA functional by the reference's EXCHANGE_CORRELATION name."""
+# ---------------------------------------------------------------------------------------------
+# GGA_PBE (src/exchangeCorrelationPotential.m:156-326, nspin = 1) on the Cyclix gradients of
+# Cychel/gradIndicesValues_cychel.m and Cychel/blochGradient_cychel.m (k = 0)
+# ---------------------------------------------------------------------------------------------
+def cyclix_gradients(S):
+    """Cartesian derivative operators on the (r, theta, z) grid, FD order 2 FDn:
+    D_x = cos(phi) d_r - sin(phi)/r d_theta, D_y = sin(phi) d_r + cos(phi)/r d_theta,
+    D_z = d_z - tau d_theta, phi = theta + tau z; zero outside the radial Dirichlet ends,
+    periodic in theta and z (Cychel/gradIndicesValues_cychel.m:1-141)."""
+    Nx, Ny, Nz, n = S.Nx, S.Ny, S.Nz, S.FDn
+    N = Nx * Ny * Nz
+    i, j, k = np.meshgrid(np.arange(Nx), np.arange(Ny), np.arange(Nz), indexing="ij")
+    i, j, k = (a.reshape(-1, order="F") for a in (i, j, k))
+    row = i + Nx * (j + Ny * k)
+    r = S.xin + i * S.dx
+    ph = j * S.dy + S.twist * (k * S.dz)
+    c, sn = np.cos(ph), np.sin(ph)
+    ops = [[], [], []]
+    for p in range(1, n + 1):
+        w = S.w1[p]
+        for sgn in (1, -1):
+            ii = i + sgn * p
+            ok = (ii >= 0) & (ii < Nx)                               # radial: Dirichlet zero ghosts
+            col = ii + Nx * (j + Ny * k)
+            for d, wt in ((0, c / S.dx), (1, sn / S.dx)):
+                ops[d].append((row[ok], col[ok], (sgn * w * wt)[ok]))
+            jj = np.mod(j + sgn * p, Ny)                             # theta: periodic (k = 0)
+            col = i + Nx * (jj + Ny * k)
+            for d, wt in ((0, -sn / (r * S.dy)), (1, c / (r * S.dy)), (2, np.full(N, -S.twist / S.dy))):
+                ops[d].append((row, col, sgn * w * wt))
+            kk = np.mod(k + sgn * p, Nz)                             # z: periodic
+            col = i + Nx * (j + Ny * kk)
+            ops[2].append((row, col, np.full(N, sgn * w / S.dz)))
+    mats = []
+    for d in range(3):
+        R = np.concatenate([a for a, _, _ in ops[d]])
+        Cc = np.concatenate([b for _, b, _ in ops[d]])
+        V = np.concatenate([v for _, _, v in ops[d]])
+        mats.append(sp.csr_matrix((V, (R, Cc)), shape=(N, N)))
+    return mats
+
+
+PBE = dict(kappa=0.804, mu=0.2195149727645171, beta=0.066725)
+
+
+def _pbe_f(rho, sigma):
+    """rho * e_xc of unpolarised PBE (Perdew, Burke, Ernzerhof, PRL 77, 3865 (1996)) with the
+    PW92 correlation of LDA_PW; written for complex arguments (complex-step derivatives)."""
+    kappa, mu, beta = PBE["kappa"], PBE["mu"], PBE["beta"]
+    gam = (1.0 - math.log(2.0)) / math.pi ** 2
+    kf = (3.0 * math.pi ** 2 * rho) ** (1.0 / 3.0)
+    ex_lda = -0.75 * (3.0 / math.pi) ** (1.0 / 3.0) * rho ** (1.0 / 3.0)
+    s2 = sigma / (4.0 * kf * kf * rho * rho)
+    Fx = 1.0 + kappa - kappa / (1.0 + mu * s2 / kappa)
+    rs = (0.75 / (math.pi * rho)) ** (1.0 / 3.0)
+    A0, a1, b1, b2, b3, b4 = 0.031091, 0.21370, 7.5957, 3.5876, 1.6382, 0.49294
+    ec = -2.0 * A0 * (1.0 + a1 * rs) * np.log(1.0 + 1.0 / (2.0 * A0 * (b1 * rs ** 0.5 + b2 * rs + b3 * rs ** 1.5 + b4 * rs * rs)))
+    ks2 = 4.0 * kf / math.pi
+    t2 = sigma / (4.0 * ks2 * rho * rho)
+    Ac = (beta / gam) / (np.exp(-ec / gam) - 1.0)
+    At2 = Ac * t2
+    H = gam * np.log(1.0 + (beta / gam) * t2 * (1.0 + At2) / (1.0 + At2 + At2 * At2))
+    return rho * (ex_lda * Fx + ec + H)
+
+
+def _pbe_parts(rho, sigma):
+    """(f, df/drho, df/dsigma) by complex-step differentiation (exact to rounding)."""
+    h = 1e-30
+    f = _pbe_f(rho, sigma).real
+    fr = _pbe_f(rho + 1j * h * rho, sigma + 0j).imag / (h * rho)
+    hs = h * (sigma + rho ** (8.0 / 3.0))            # sigma's natural scale; nonzero where sigma = 0
+    fs = _pbe_f(rho + 0j, sigma + 1j * hs).imag / hs
+    return f, fr, fs
+
+
+def gga_pbe(rho, grads):
+    """(Vxc, e_xc) of src/exchangeCorrelationPotential.m:156-326: gradients of the clipped density,
+    v = d(rho e)/d rho, and Vxc = v - sum_i D_i (2 d(rho e)/d sigma D_i rho)."""
+    rho = np.where(rho < XC_RHOTOL, XC_RHOTOL, rho)
+    d = [G @ rho for G in grads]
+    sigma = d[0] * d[0] + d[1] * d[1] + d[2] * d[2]
+    f, fr, fs = _pbe_parts(rho, sigma)
+    V = fr - sum(G @ (2.0 * fs * di) for G, di in zip(grads, d))
+    return V, f / rho
+
+
+def xc_functions(name, S=None):
+    """(potential(rho), energy(rho, W)) of an XC functional by the reference's EXCHANGE_CORRELATION name."""
     if name == "LDA_PW":
         return lda_pw_potential, lda_pw_energy
     if name == "LDA_PZ":
         return lda_pz_potential, lda_pz_energy
-    raise ValueError(f"exchange-correlation {name}: the oracle implements LDA_PW and LDA_PZ")
+    if name == "GGA_PBE":
+        grads = cyclix_gradients(S)
+
+        def energy(rho, W):
+            e = gga_pbe(rho, grads)[1]
+            rho_c = np.where(rho < XC_RHOTOL, XC_RHOTOL, rho)
+            return float(np.sum(e * rho_c * W))          # src/evaluateTotalEnergy.m:61-62
+        return (lambda rho: gga_pbe(rho, grads)[0]), energy
+    raise ValueError(f"exchange-correlation {name}: the oracle implements LDA_PW, LDA_PZ and GGA_PBE")
 
 
 # ---------------------------------------------------------------------------------------------
@@ -237,7 +332,7 @@ def scf(S, psis, blocks, scf_tol=1e-6, poisson_tol=None, rhoTrigger=4, max_scf=1
     """
     N = S.N
     T_type = getattr(S, "elec_T_type", 1)
-    vxc_fn, exc_fn = xc_functions(S.extra.get("xc", "LDA_PW"))
+    vxc_fn, exc_fn = xc_functions(S.extra.get("xc", "LDA_PW"), S)
     poisson_tol = poisson_tol if poisson_tol is not None else 0.01 * scf_tol
     P = PoissonOperator(S)
     wk = np.asarray(S.wkpt)

@@ -127,3 +127,46 @@ def test_lda_pz_close_to_pw():
         a = OS.lda_pz_energy(np.array([r]), W) / r
         b = OS.lda_pw_energy(np.array([r]), W) / r
         assert abs(a - b) < 3e-3
+
+
+def test_pbe_reduces_to_lda_pw_for_a_uniform_density():
+    # sigma = 0: F_x = 1 and H = 0, so PBE is the PW92 LDA (same correlation parameters)
+    rho = np.geomspace(1e-4, 5.0, 30)
+    f, fr, fs = OS._pbe_parts(rho, np.zeros_like(rho))
+    e_lda = np.array([OS.lda_pw_energy(np.array([r]), np.ones(1)) for r in rho])
+    assert np.allclose(f, e_lda, rtol=1e-12)
+    assert np.allclose(fr, OS.lda_pw_potential(rho), rtol=1e-10)
+    # second-order gradient terms at sigma = 0: exchange -3 mu / (16 pi k_F rho), correlation
+    # beta pi / (16 k_F rho); PBE's mu = beta pi^2 / 3 makes them cancel
+    kf = (3 * np.pi ** 2 * rho) ** (1 / 3)
+    beta, mu = OS.PBE["beta"], OS.PBE["mu"]
+    assert np.allclose(fs * 16 * kf * rho, np.pi * beta - 3 * mu / np.pi, rtol=0, atol=1e-9)
+    assert abs(np.pi * beta - 3 * mu / np.pi) < 2e-5
+
+
+@pytest.mark.parametrize("rho,sigma", [(0.01, 1e-5), (0.2, 0.03), (1.5, 2.0)])
+def test_pbe_complex_step_derivatives(rho, sigma):
+    f0 = lambda r, s: OS._pbe_f(np.array([r]), np.array([s]))[0]
+    f, fr, fs = (v[0] for v in OS._pbe_parts(np.array([rho]), np.array([sigma])))
+    hr, hs = 1e-5 * rho, 1e-5 * sigma
+    assert abs(fr - (f0(rho + hr, sigma) - f0(rho - hr, sigma)) / (2 * hr)) < 1e-7 * max(1, abs(fr))
+    assert abs(fs - (f0(rho, sigma + hs) - f0(rho, sigma - hs)) / (2 * hs)) < 1e-6 * max(1, abs(fs))
+
+
+def test_cyclix_gradients_on_a_smooth_field():
+    # f = x^2 + y^2 + sin(2 pi z / L3) is periodic in theta and z: D_x f = 2x, D_y f = 2y,
+    # D_z f = (2 pi / L3) cos(2 pi z / L3), away from the radial Dirichlet ends, on a cyclic and on
+    # a helical cell (Cychel/gradIndicesValues_cychel.m)
+    for twist in (0.0, 0.05):
+        S = bare_cell(30, 12, 16, twist=twist)
+        G = OS.cyclix_gradients(S)
+        r = S.xin + np.arange(S.Nx) * S.dx
+        R, T, Z = np.meshgrid(r, np.arange(S.Ny) * S.dy, np.arange(S.Nz) * S.dz, indexing="ij")
+        R, T, Z = (a.reshape(-1, order="F") for a in (R, T, Z))
+        X, Y = R * np.cos(T + twist * Z), R * np.sin(T + twist * Z)
+        k = 2 * np.pi / S.L3
+        f = X * X + Y * Y + np.sin(k * Z)
+        inner = (R > r[S.FDn]) & (R < r[-S.FDn - 1])
+        assert np.allclose((G[0] @ f)[inner], 2 * X[inner], atol=1e-8)
+        assert np.allclose((G[1] @ f)[inner], 2 * Y[inner], atol=1e-8)
+        assert np.allclose((G[2] @ f)[inner], k * np.cos(k * Z[inner]), atol=1e-7)
