@@ -379,4 +379,5 @@ def scf(S, psis, blocks, scf_tol=1e-6, poisson_tol=None, rhoTrigger=4, max_scf=1
                 Veff_temp = Veff.copy()
             count_scf += 1
         count += 1
-    return dict(Etotal=Etot, EigVal=EigVal, lambda_f=lam_f, rho=rho, Veff=Veff, n_scf=count_scf - 1, history=hist, psis=psis)
+    return dict(Etotal=Etot, EigVal=EigVal, lambda_f=lam_f, occ=occ, rho=rho, phi=phi, Veff=Veff, n_scf=count_scf - 1,
+                history=hist, psis=psis)

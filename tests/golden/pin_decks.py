@@ -42,7 +42,22 @@ def out_values(out_path):
     radii = re.search(r"Pseudocharge radii of atom type 1\s*:\s*([0-9.]+)\s+([0-9.]+)\s+([0-9.]+)", txt)
     nscf = re.search(r"Total number of SCF:\s*(\d+)", txt)
     last_err = re.findall(r"^\d+\s+[-+0-9.Ee]+\s+([0-9.Ee+-]+)\s+[0-9.]+\s*$", txt, re.M)
-    return dict(free_energy_per_atom=num(r"Free energy per atom"),
+    static = os.path.splitext(out_path)[0] + ".static"
+    forces = None
+    if os.path.exists(static):
+        st = open(static).read().split("Atomic forces (Ha/Bohr):")
+        if len(st) > 1:
+            rows = []
+            for ln in st[1].strip().splitlines():
+                parts = ln.split()
+                if len(parts) != 3:
+                    break
+                try:
+                    rows.append([float(v) for v in parts])
+                except ValueError:
+                    break
+            forces = rows or None
+    return dict(forces=forces, free_energy_per_atom=num(r"Free energy per atom"),
                 self_and_correction=num(r"Self and correction energy"),
                 fermi_level=num(r"Fermi level"),
                 radii=[float(radii.group(i)) for i in (1, 2, 3)] if radii else None,
@@ -112,11 +127,16 @@ def pin(deck_rel, scf_tol=1e-6, max_scf=60, root=REFERENCE, gpu=None):
     def log(it, e, err):
         hist.append((it, float(e), float(err)))
         print(f"  SCF {it:3d}  E = {e:.10f} Ha/atom  err = {err:.3e}  ({time.time() - t0:.0f} s)", flush=True)
+    forces = None
     if gpu:
         res = _gpu_scf(S, blocks, psis, gpu, scf_tol, d.poisson_tol, max_scf, log)
     else:
         from oracle import scf as OS
+        from oracle.forces import atomic_forces
         res = OS.scf(S, psis, blocks, scf_tol=scf_tol, poisson_tol=d.poisson_tol, max_scf=max_scf, log=log)
+        if ref.get("forces") is not None:
+            F, _ = atomic_forces(d, res["psis"], res["occ"], res["phi"])
+            forces = F.tolist()
     E = res["Etotal"] / S.n_atm
     # the energy when the oracle's SCF error first fell to the reference's final error
     e_at_ref = next((e for (_, e, err) in hist if err <= ref["last_scf_error"]), None) if ref["last_scf_error"] else None
@@ -128,6 +148,9 @@ def pin(deck_rel, scf_tol=1e-6, max_scf=60, root=REFERENCE, gpu=None):
                            n_scf=res["n_scf"], scf_tol=scf_tol, energy_at_reference_error=e_at_ref,
                            history=hist, wall_s=round(time.time() - t0, 1)),
                diff_free_energy_per_atom=E - ref["free_energy_per_atom"],
+               forces=forces,
+               max_diff_force=(float(np.max(np.abs(np.array(forces) - np.array(ref["forces"]))))
+                               if forces is not None else None),
                diff_self_and_correction=(S.E_corr - S.Eself) - ref["self_and_correction"])
     return rec
 
