@@ -115,8 +115,9 @@ def _rot_pow(R, p):
 
 
 def atomic_forces(d, psis, occ, phi):
-    """Forces (n_atm, 3) in Ha/bohr of the converged SCF of a loaded deck ``d``: ``psis`` and ``occ``
-    per Bloch block (W-normalised psi, N x Ns), ``phi`` the electrostatic potential."""
+    """Drift-free forces (n_atm, 3) in Ha/bohr of the converged SCF of a loaded deck ``d``: ``psis``
+    and ``occ`` per Bloch block (W-normalised psi, N x Ns), ``phi`` the electrostatic potential.
+    Also returns the three terms before the drift correction."""
     S, pc = d.S, d.pseudo
     n = S.FDn
     ent = _grad_entries(S)
@@ -183,4 +184,8 @@ def atomic_forces(d, psis, occ, phi):
                 i2 = -(PsiW @ DC).T
                 fk[J, q] = float(A.gamma_Jl @ np.real(i1 * i2) @ occ[b])
         F_nl -= S.occfac * 2 * S.wkpt[b] * fk
-    return F_loc + F_cor + F_nl, {"local": F_loc, "correction": F_cor, "nonlocal": F_nl}
+    F = F_loc + F_cor + F_nl
+    # drift-free forces: the mean force is removed along z, the translation a Cyclix cell has
+    # (src/electronicGroundState.m:108-115)
+    F[:, 2] -= F[:, 2].mean()
+    return F, {"local": F_loc, "correction": F_cor, "nonlocal": F_nl}
