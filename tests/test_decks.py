@@ -18,8 +18,9 @@ compared only where the .out was written by the committed radius rule (rb_y = ac
 Decks whose numbers still differ (their .ion or pseudopotential changed after the run, e.g. the
 relaxation deck tests/Cyclix/CNT_relax) are not listed.
 
-The full SCF of the LDA deck is pinned by tests/golden/pin_decks.py, which writes
-tests/golden/deck_pins.json (checked below).  The reference tree is read where it exists; the
+The full SCF of six decks (cyclic and helical; LDA_PW, LDA_PZ and GGA_PBE; Gaussian and
+Fermi-Dirac) and the forces of the two helical ones are pinned by tests/golden/pin_decks.py,
+which writes tests/golden/deck_pins.json (checked below).  The reference tree is read where it exists; the
 tests skip elsewhere.
 """
 import json
@@ -37,10 +38,11 @@ DECKS = [("LDA_CNT/C.inpt", True), ("GGA_CNT_sg15/C.inpt", True), ("tests/MoS2/M
          ("tests/Cyclix/CNT_ABINITmatch/C.inpt", False), ("tests/Cyclix/CNT_chiral/C.inpt", False),
          ("tests/phonon/Si_1/Si.inpt", False), ("tests/phonon/Si_2/Si.inpt", False)]
 # free energy per atom, oracle SCF vs the .out, by how far each reference run converged:
-# LDA_CNT stopped at SCF error 8e-5 (TOL_SCF 1e-4), phonon/Si_2 below 1e-5, CNT_chiral and
-# phonon/Si_1 (both helical, Fermi-Dirac) at ~1e-6
-PIN_TOL = {"LDA_CNT/C.inpt": 1e-5, "tests/Cyclix/CNT_chiral/C.inpt": 1e-6,
-           "tests/phonon/Si_1/Si.inpt": 1e-6, "tests/phonon/Si_2/Si.inpt": 2e-6}
+# LDA_CNT and GGA_CNT_sg15 stopped at SCF error ~6e-5 (TOL_SCF 1e-4), phonon/Si_2 below 1e-5,
+# CNT_chiral, phonon/Si_1 (helical) and CNT_ABINITmatch at ~1e-6
+PIN_TOL = {"LDA_CNT/C.inpt": 1e-5, "GGA_CNT_sg15/C.inpt": 1e-5, "tests/Cyclix/CNT_chiral/C.inpt": 1e-6,
+           "tests/phonon/Si_1/Si.inpt": 1e-6, "tests/phonon/Si_2/Si.inpt": 2e-6,
+           "tests/Cyclix/CNT_ABINITmatch/C.inpt": 1e-6}
 
 
 def _out(inpt):
@@ -154,7 +156,6 @@ def test_scf_pin_record(deck, tol):
     assert abs(rec["diff_free_energy_per_atom"]) <= tol, rec["diff_free_energy_per_atom"]
 
 
-
 def test_split_projector_columns_is_the_same_operator(loaded):
     """psp8 atoms with 8 projector columns go to the GPU library as two 4-column atoms at the same
     position (the kernels hold 4); the KB term is a sum over columns, so H is unchanged (checked
@@ -181,3 +182,19 @@ def test_split_projector_columns_is_the_same_operator(loaded):
     # atoms that fit are passed through unchanged
     same, org = split_projector_columns(atoms, 4)
     assert same == atoms and org == list(range(len(atoms)))
+
+
+@pytest.mark.parametrize("deck", ["tests/Cyclix/CNT_chiral/C.inpt", "tests/phonon/Si_1/Si.inpt"])
+def test_force_pin_record(deck):
+    """Drift-free atomic forces of the oracle (oracle/forces.py, src/atomicForce.m) at the converged
+    SCF of a helical deck against the forces the reference printed in the deck's .static file."""
+    path = os.path.join(HERE, "golden", "deck_pins.json")
+    recs = json.load(open(path)) if os.path.exists(path) else {}
+    rec = recs.get(deck)
+    if not rec or rec.get("forces") is None:
+        pytest.skip("no force record for this deck")
+    F = np.array(rec["forces"])
+    Fr = np.array(rec["reference"]["forces"])
+    assert F.shape == Fr.shape
+    # both SCFs converged to ~1e-6; forces are first order in the density error
+    assert np.max(np.abs(F - Fr)) <= 2e-5, np.max(np.abs(F - Fr))
