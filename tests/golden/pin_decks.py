@@ -3,7 +3,8 @@
 For each deck, the reference's input files (.inpt, .ion, .psp8) are loaded by
 ``cyclix_msparc_gb300.deck`` and the oracle SCF (oracle/scf.py) runs from the atomic density
 guess.  The free energy per atom, the self and correction energy and the pseudocharge radii are
-compared with the numbers the reference printed into the deck's .out file.  The result is
+compared with the numbers the reference printed into the deck's .out file, and, where the deck's
+.static file holds them, the drift-free atomic forces (oracle/forces.py).  The result is
 written to ``deck_pins.json`` next to this script; tests/test_decks.py checks the record and
 re-derives the fast quantities (radii, self and correction energy) from the deck files.
 
