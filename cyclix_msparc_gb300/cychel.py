@@ -130,6 +130,38 @@ class CyclixS:
         return self.xin + self.L1
 
 
+def periodic_images(S, x0: float, y0: float, z0: float, rby: float, rbz: float) -> list:
+    """Periodic images of an atom whose box of half-widths (., rby, rbz) may reach the cell, in the
+    reference's ndgrid order (theta before z; src/calculate_b_guessRho_Eself.m:38-69,
+    src/calculate_nloc_projector.m:50-81).  Theta images only for a periodic theta, z images only
+    for a periodic z."""
+    nyl = math.floor((y0 + rby) / S.L2) if S.BCy == 0 else 0
+    nyr = math.floor((S.L2 - y0 + rby - S.dy) / S.L2) if S.BCy == 0 else 0
+    nzl = math.floor((z0 + rbz) / S.L3) if S.BCz == 0 else 0
+    nzr = math.floor((S.L3 - z0 + rbz - S.dz) / S.L3) if S.BCz == 0 else 0
+    return [(x0, y0 + j * S.L2, z0 + k * S.L3) for k in range(-nzl, nzr + 1) for j in range(-nyl, nyr + 1)]
+
+
+def image_reaches_cell(S, x0i: float, y0i: float, z0i: float, rb) -> bool:
+    """Whether the box of half-widths rb around an image overlaps the cell
+    (src/calculate_nloc_projector.m:99-102; yin = zin = 0)."""
+    rbx, rby, rbz = rb
+    in_x = ((x0i - S.xin) - S.L1 + S.dx <= rbx) or (abs(x0i - S.xin) <= rbx)
+    in_y = (y0i - S.L2 + S.dy <= rby) or (abs(y0i) <= rby)
+    in_z = (z0i - S.L3 + S.dz <= rbz) or (abs(z0i) <= rbz)
+    return in_x and in_y and in_z
+
+
+def clipped_box(S, x0i: float, y0i: float, z0i: float, rb) -> tuple:
+    """1-based (start, end) grid index ranges of the box of half-widths rb around an image,
+    clipped to the cell (src/calculate_b_guessRho_Eself.m:81-103); empty when end < start."""
+    rbx, rby, rbz = rb
+    ii = (max(math.ceil(((x0i - S.xin) - rbx) / S.dx) + 1, 1), min(math.floor(((x0i - S.xin) + rbx) / S.dx) + 1, S.Nx))
+    jj = (max(math.ceil((y0i - rby) / S.dy) + 1, 1), min(math.floor((y0i + rby) / S.dy) + 1, S.Ny))
+    kk = (max(math.ceil((z0i - rbz) / S.dz) + 1, 1), min(math.floor((z0i + rbz) / S.dz) + 1, S.Nz))
+    return ii, jj, kk
+
+
 def split_projector_columns(atoms: list, width: int = 4) -> tuple[list, list]:
     """Atoms whose projector columns fit ``width``.
 

@@ -27,8 +27,8 @@ from dataclasses import dataclass, field
 import numpy as np
 from scipy.interpolate import CubicSpline
 
-from .cychel import (AtomNL, CyclixS, RcImage, cyclix_kpoints, fd_weights, intg_weights, noncart2cart,
-                     real_ylm, rot_z)
+from .cychel import (AtomNL, CyclixS, RcImage, clipped_box, cyclix_kpoints, fd_weights, image_reaches_cell,
+                     intg_weights, noncart2cart, periodic_images, real_ylm, rot_z)
 
 HARTREE_EV = 27.211386245988        # src/initialization.m:947 (Cst)
 RC_REF = 0.5                        # reference pseudopotential cut-off, src/initialization.m:971
@@ -305,24 +305,8 @@ def pseudocharge_radii(S, psp: Psp8, xmax_at: float, xvac: float, tol: float) ->
     return rbx, rby, rbz
 
 
-def _images(S, x0, y0, z0, rby, rbz):
-    """Periodic images whose rb box may reach the cell (src/calculate_b_guessRho_Eself.m:38-69),
-    in ndgrid order (theta fastest after r, then z)."""
-    nyl = math.floor((y0 + rby) / S.L2) if S.BCy == 0 else 0
-    nyr = math.floor((S.L2 - y0 + rby - S.dy) / S.L2) if S.BCy == 0 else 0
-    nzl = math.floor((z0 + rbz) / S.L3) if S.BCz == 0 else 0
-    nzr = math.floor((S.L3 - z0 + rbz - S.dz) / S.L3) if S.BCz == 0 else 0
-    return [(x0, y0 + j * S.L2, z0 + k * S.L3) for k in range(-nzl, nzr + 1) for j in range(-nyl, nyr + 1)]
-
-
-def _box(S, x0i, y0i, z0i, rb):
-    """1-based index ranges of the rb box of an image, clipped to the cell
-    (src/calculate_b_guessRho_Eself.m:81-103)."""
-    rbx, rby, rbz = rb
-    ii = (max(math.ceil(((x0i - S.xin) - rbx) / S.dx) + 1, 1), min(math.floor(((x0i - S.xin) + rbx) / S.dx) + 1, S.Nx))
-    jj = (max(math.ceil((y0i - rby) / S.dy) + 1, 1), min(math.floor((y0i + rby) / S.dy) + 1, S.Ny))
-    kk = (max(math.ceil((z0i - rbz) / S.dz) + 1, 1), min(math.floor((z0i + rbz) / S.dz) + 1, S.Nz))
-    return ii, jj, kk
+_images = periodic_images        # image enumeration and box clipping shared with the synthetic systems
+_box = clipped_box
 
 
 def pseudocharges(S, psps: list, atom_type: np.ndarray, rbs: list) -> dict:
@@ -398,10 +382,7 @@ def projectors(S, psps: list, atom_type: np.ndarray, rbs: list) -> list:
         splines = {(l, p): CubicSpline(psp.r, psp.proj[l][:, p]) for (l, p, _) in cols}
         images = []
         for (x0i, y0i, z0i) in _images(S, x0, y0, z0, rb[1], rb[2]):
-            in_x = ((x0i - S.xin) - S.L1 + S.dx <= rb[0]) or (abs(x0i - S.xin) <= rb[0])
-            in_y = (y0i - S.L2 + S.dy <= rb[1]) or (abs(y0i) <= rb[1])
-            in_z = (z0i - S.L3 + S.dz <= rb[2]) or (abs(z0i) <= rb[2])
-            if not (in_x and in_y and in_z):
+            if not image_reaches_cell(S, x0i, y0i, z0i, rb):
                 continue
             (is_, ie), (js, je), (ks, ke) = _box(S, x0i, y0i, z0i, rb)
             if ie < is_ or je < js or ke < ks:

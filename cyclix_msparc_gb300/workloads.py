@@ -26,8 +26,8 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from .cychel import (AtomNL, CyclixS, RcImage, cell_type, fd_weights, intg_weights,
-                     noncart2cart, real_ylm, rot_z)
+from .cychel import (AtomNL, CyclixS, RcImage, cell_type, clipped_box, fd_weights, image_reaches_cell,
+                     intg_weights, noncart2cart, periodic_images, real_ylm, rot_z)
 
 
 @dataclass(frozen=True)
@@ -157,62 +157,47 @@ def nloc_projectors(S: CyclixS, rc: float, gammas: np.ndarray, lmax: int = 1) ->
         rcx = rc
         rcy = math.asin(min(1.0, rc / max(x0 - rc, 1e-12))) + abs(S.twist) * rc
         rcz = rc
-        nyl = math.floor((y0 + rcy) / S.L2) if S.BCy == 0 else 0
-        nyr = math.floor((S.L2 - y0 + rcy - S.dy) / S.L2) if S.BCy == 0 else 0
-        nzl = math.floor((z0 + rcz) / S.L3) if S.BCz == 0 else 0
-        nzr = math.floor((S.L3 - z0 + rcz - S.dz) / S.L3) if S.BCz == 0 else 0
-        yy_img = np.arange(-nyl, nyr + 1) * S.L2 + y0
-        zz_img = np.arange(-nzl, nzr + 1) * S.L3 + z0
+        rb = (rcx, rcy, rcz)
         images = []
-        for z0i in zz_img:          # ndgrid order: x fastest, then y, then z
-            for y0i in yy_img:
-                x0i = x0
-                in_x = ((x0i - S.xin) - S.L1 + S.dx <= rcx) or (abs(x0i - S.xin) <= rcx)
-                in_y = ((y0i - 0.0) - S.L2 + S.dy <= rcy) or (abs(y0i - 0.0) <= rcy)
-                in_z = ((z0i - 0.0) - S.L3 + S.dz <= rcz) or (abs(z0i - 0.0) <= rcz)
-                if not (in_x and in_y and in_z):
-                    continue
-                ii_s = max(math.ceil(((x0i - S.xin) - rcx) / S.dx) + 1, 1)
-                ii_e = min(math.floor(((x0i - S.xin) + rcx) / S.dx) + 1, S.Nx)
-                jj_s = max(math.ceil((y0i - rcy) / S.dy) + 1, 1)
-                jj_e = min(math.floor((y0i + rcy) / S.dy) + 1, S.Ny)
-                kk_s = max(math.ceil((z0i - rcz) / S.dz) + 1, 1)
-                kk_e = min(math.floor((z0i + rcz) / S.dz) + 1, S.Nz)
-                if ii_e < ii_s or jj_e < jj_s or kk_e < kk_s:
-                    continue
-                ii = np.arange(ii_s, ii_e + 1)
-                jj = np.arange(jj_s, jj_e + 1)
-                kk = np.arange(kk_s, kk_e + 1)
-                I3, J3, K3 = np.meshgrid(ii, jj, kk, indexing="ij")
-                I3 = I3.reshape(-1, order="F")
-                J3 = J3.reshape(-1, order="F")
-                K3 = K3.reshape(-1, order="F")
-                XX = S.xin + (I3 - 1) * S.dx
-                YY = (J3 - 1) * S.dy
-                ZZ = (K3 - 1) * S.dz
-                pos = (K3 - 1) * S.Nx * S.Ny + (J3 - 1) * S.Nx + I3
-                node_c = noncart2cart(S, np.stack([XX, YY, ZZ], axis=1))
-                atm_c = noncart2cart(S, np.array([[x0i, y0i, z0i]]))[0]
-                disp = node_c - atm_c
-                dd = np.sqrt((disp ** 2).sum(axis=1))
-                inb = dd <= rc
-                if not inb.any():
-                    continue
-                disp = disp[inb]
-                dd = dd[inb]
-                fac1 = int(round((y0 - y0i) / S.L2))
-                fac2 = int(round((z0 - z0i) / S.L3))
-                ROT = np.linalg.matrix_power(RotM1, fac1) @ np.linalg.matrix_power(RotM2, fac2) \
-                    if fac1 >= 0 and fac2 >= 0 else _rot_pow(RotM1, fac1) @ _rot_pow(RotM2, fac2)
-                P = (ROT @ disp.T).T
-                chi = np.zeros((dd.shape[0], angnum))
-                col = 0
-                for l in range(lmax + 1):
-                    f = _radial(l, dd, sig)
-                    for m in range(-l, l + 1):
-                        chi[:, col] = f * real_ylm(l, m, P[:, 0], P[:, 1], P[:, 2])
-                        col += 1
-                images.append(RcImage(np.array([x0i, y0i, z0i]), pos[inb].astype(np.int64), chi))
+        for (x0i, y0i, z0i) in periodic_images(S, x0, y0, z0, rcy, rcz):
+            if not image_reaches_cell(S, x0i, y0i, z0i, rb):
+                continue
+            (ii_s, ii_e), (jj_s, jj_e), (kk_s, kk_e) = clipped_box(S, x0i, y0i, z0i, rb)
+            if ii_e < ii_s or jj_e < jj_s or kk_e < kk_s:
+                continue
+            ii = np.arange(ii_s, ii_e + 1)
+            jj = np.arange(jj_s, jj_e + 1)
+            kk = np.arange(kk_s, kk_e + 1)
+            I3, J3, K3 = np.meshgrid(ii, jj, kk, indexing="ij")
+            I3 = I3.reshape(-1, order="F")
+            J3 = J3.reshape(-1, order="F")
+            K3 = K3.reshape(-1, order="F")
+            XX = S.xin + (I3 - 1) * S.dx
+            YY = (J3 - 1) * S.dy
+            ZZ = (K3 - 1) * S.dz
+            pos = (K3 - 1) * S.Nx * S.Ny + (J3 - 1) * S.Nx + I3
+            node_c = noncart2cart(S, np.stack([XX, YY, ZZ], axis=1))
+            atm_c = noncart2cart(S, np.array([[x0i, y0i, z0i]]))[0]
+            disp = node_c - atm_c
+            dd = np.sqrt((disp ** 2).sum(axis=1))
+            inb = dd <= rc
+            if not inb.any():
+                continue
+            disp = disp[inb]
+            dd = dd[inb]
+            fac1 = int(round((y0 - y0i) / S.L2))
+            fac2 = int(round((z0 - z0i) / S.L3))
+            ROT = np.linalg.matrix_power(RotM1, fac1) @ np.linalg.matrix_power(RotM2, fac2) \
+                if fac1 >= 0 and fac2 >= 0 else _rot_pow(RotM1, fac1) @ _rot_pow(RotM2, fac2)
+            P = (ROT @ disp.T).T
+            chi = np.zeros((dd.shape[0], angnum))
+            col = 0
+            for l in range(lmax + 1):
+                f = _radial(l, dd, sig)
+                for m in range(-l, l + 1):
+                    chi[:, col] = f * real_ylm(l, m, P[:, 0], P[:, 1], P[:, 2])
+                    col += 1
+            images.append(RcImage(np.array([x0i, y0i, z0i]), pos[inb].astype(np.int64), chi))
         g = np.concatenate([np.full(2 * l + 1, gammas[J, l]) for l in range(lmax + 1)])
         atoms.append(AtomNL(angnum, g, images))
     return atoms
