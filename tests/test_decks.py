@@ -184,10 +184,15 @@ def test_split_projector_columns_is_the_same_operator(loaded):
     assert same == atoms and org == list(range(len(atoms)))
 
 
-@pytest.mark.parametrize("deck", ["tests/Cyclix/CNT_chiral/C.inpt", "tests/phonon/Si_1/Si.inpt"])
-def test_force_pin_record(deck):
+# forces, oracle vs the .static file: the helical decks' reference runs converged to ~1e-6, the
+# LDA_CNT run stopped at SCF error 8e-5 (forces are first order in the density error)
+FORCE_TOL = {"tests/Cyclix/CNT_chiral/C.inpt": 2e-5, "tests/phonon/Si_1/Si.inpt": 2e-5, "LDA_CNT/C.inpt": 2e-4}
+
+
+@pytest.mark.parametrize("deck,tol", FORCE_TOL.items())
+def test_force_pin_record(deck, tol):
     """Drift-free atomic forces of the oracle (oracle/forces.py, src/atomicForce.m) at the converged
-    SCF of a helical deck against the forces the reference printed in the deck's .static file."""
+    SCF of a deck against the forces the reference printed in the deck's .static file."""
     path = os.path.join(HERE, "golden", "deck_pins.json")
     recs = json.load(open(path)) if os.path.exists(path) else {}
     rec = recs.get(deck)
@@ -196,5 +201,4 @@ def test_force_pin_record(deck):
     F = np.array(rec["forces"])
     Fr = np.array(rec["reference"]["forces"])
     assert F.shape == Fr.shape
-    # both SCFs converged to ~1e-6; forces are first order in the density error
-    assert np.max(np.abs(F - Fr)) <= 2e-5, np.max(np.abs(F - Fr))
+    assert np.max(np.abs(F - Fr)) <= tol, np.max(np.abs(F - Fr))
