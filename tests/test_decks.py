@@ -185,8 +185,10 @@ def test_split_projector_columns_is_the_same_operator(loaded):
 
 
 # forces, oracle vs the .static file: the helical decks' reference runs converged to ~1e-6, the
-# LDA_CNT run stopped at SCF error 8e-5 (forces are first order in the density error)
-FORCE_TOL = {"tests/Cyclix/CNT_chiral/C.inpt": 2e-5, "tests/phonon/Si_1/Si.inpt": 2e-5, "LDA_CNT/C.inpt": 2e-4}
+# LDA_CNT and GGA_CNT_sg15 runs stopped at SCF error ~6e-5 (forces are first order in the density
+# error)
+FORCE_TOL = {"tests/Cyclix/CNT_chiral/C.inpt": 2e-5, "tests/phonon/Si_1/Si.inpt": 2e-5, "LDA_CNT/C.inpt": 2e-4,
+             "GGA_CNT_sg15/C.inpt": 2e-4}
 
 
 @pytest.mark.parametrize("deck,tol", FORCE_TOL.items())
