@@ -40,7 +40,8 @@ DECKS = [("LDA_CNT/C.inpt", True), ("GGA_CNT_sg15/C.inpt", True), ("tests/MoS2/M
 # free energy per atom, oracle SCF vs the .out, by how far each reference run converged:
 # LDA_CNT and GGA_CNT_sg15 stopped at SCF error ~6e-5 (TOL_SCF 1e-4), phonon/Si_2 below 1e-5,
 # CNT_chiral, phonon/Si_1 (helical) and CNT_ABINITmatch at ~1e-6
-PIN_TOL = {"LDA_CNT/C.inpt": 1e-5, "GGA_CNT_sg15/C.inpt": 1e-5, "tests/Cyclix/CNT_chiral/C.inpt": 1e-6,
+PIN_TOL = {"LDA_CNT/C.inpt": 1e-5, "GGA_CNT_sg15/C.inpt": 1e-5, "GGA_wrong_SG15/C.inpt": 1e-5,
+           "tests/Cyclix/CNT_chiral/C.inpt": 1e-6,
            "tests/phonon/Si_1/Si.inpt": 1e-6, "tests/phonon/Si_2/Si.inpt": 2e-6,
            "tests/Cyclix/CNT_ABINITmatch/C.inpt": 1e-6}
 
@@ -187,8 +188,11 @@ def test_split_projector_columns_is_the_same_operator(loaded):
 # forces, oracle vs the .static file: the helical decks' reference runs converged to ~1e-6, the
 # LDA_CNT and GGA_CNT_sg15 runs stopped at SCF error ~6e-5 (forces are first order in the density
 # error)
+# GGA_wrong_SG15 and GGA_CNT_sg15 are the same deck run twice; the committed GGA potential
+# (src/exchangeCorrelationPotential.m:362, scalar gradient operators in the divergence) matches the
+# first, while the second's forces follow the commented-out vector divergence of :361
 FORCE_TOL = {"tests/Cyclix/CNT_chiral/C.inpt": 2e-5, "tests/phonon/Si_1/Si.inpt": 2e-5, "LDA_CNT/C.inpt": 2e-4,
-             "GGA_CNT_sg15/C.inpt": 2e-4}
+             "GGA_wrong_SG15/C.inpt": 2e-4}
 
 
 @pytest.mark.parametrize("deck,tol", FORCE_TOL.items())
