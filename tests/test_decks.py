@@ -15,8 +15,9 @@ the parameters they ran with, and the deck is loaded with those (tests/Cyclix/CN
 for example, ran on FD_GRID 120 61 8 against 140 70 15 in its .inpt).  Pseudocharge radii are
 compared only where the .out was written by the committed radius rule (rb_y = acos(1 - rb_z^2 /
 (2 r^2)) + tau rb_z / 2); the energies do not depend on the radii once b has converged.
-Decks whose numbers still differ (their .ion or pseudopotential changed after the run, e.g. the
-relaxation deck tests/Cyclix/CNT_relax) are not listed.
+Decks whose .out does not describe a run of today's deck files are not listed: the relaxation
+deck tests/Cyclix/CNT_relax (its first step ran on another cell length), and H2O_tube and the GGA
+MoS2 tubes (not traced).
 
 The full SCF of six decks (cyclic and helical; LDA_PW, LDA_PZ and GGA_PBE; Gaussian and
 Fermi-Dirac) and the forces of the two helical ones are pinned by tests/golden/pin_decks.py,
