@@ -20,8 +20,8 @@ deck tests/Cyclix/CNT_relax (its first step ran on another cell length), and H2O
 MoS2 tubes (not traced).
 
 The full SCF of six decks (cyclic and helical; LDA_PW, LDA_PZ and GGA_PBE; Gaussian and
-Fermi-Dirac) and the forces of the two helical ones are pinned by tests/golden/pin_decks.py,
-which writes tests/golden/deck_pins.json (checked below).  The reference tree is read where it exists; the
+Fermi-Dirac) and their forces are pinned by tests/golden/pin_decks.py, which writes
+tests/golden/deck_pins.json (checked below).  The reference tree is read where it exists; the
 tests skip elsewhere.
 """
 import json
@@ -192,8 +192,8 @@ def test_split_projector_columns_is_the_same_operator(loaded):
 # GGA_wrong_SG15 and GGA_CNT_sg15 are the same deck run twice; the committed GGA potential
 # (src/exchangeCorrelationPotential.m:362, scalar gradient operators in the divergence) matches the
 # first, while the second's forces follow the commented-out vector divergence of :361
-FORCE_TOL = {"tests/Cyclix/CNT_chiral/C.inpt": 2e-5, "tests/phonon/Si_1/Si.inpt": 2e-5, "LDA_CNT/C.inpt": 2e-4,
-             "GGA_wrong_SG15/C.inpt": 2e-4}
+FORCE_TOL = {"tests/Cyclix/CNT_chiral/C.inpt": 2e-5, "tests/phonon/Si_1/Si.inpt": 2e-5, "tests/phonon/Si_2/Si.inpt": 2e-5,
+             "LDA_CNT/C.inpt": 2e-4, "GGA_wrong_SG15/C.inpt": 2e-4}
 
 
 @pytest.mark.parametrize("deck,tol", FORCE_TOL.items())
