@@ -193,6 +193,7 @@ def test_split_projector_columns_is_the_same_operator(loaded):
 # (src/exchangeCorrelationPotential.m:362, scalar gradient operators in the divergence) matches the
 # first, while the second's forces follow the commented-out vector divergence of :361
 FORCE_TOL = {"tests/Cyclix/CNT_chiral/C.inpt": 2e-5, "tests/phonon/Si_1/Si.inpt": 2e-5, "tests/phonon/Si_2/Si.inpt": 2e-5,
+             "tests/Cyclix/CNT_ABINITmatch/C.inpt": 2e-5,
              "LDA_CNT/C.inpt": 2e-4, "GGA_wrong_SG15/C.inpt": 2e-4}
 
 
