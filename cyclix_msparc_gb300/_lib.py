@@ -20,7 +20,9 @@ PREC = {"fp64": CX_PREC_FP64, "mixed": CX_PREC_MIXED}
 EXPORTS = ["cx_create", "cx_destroy", "cx_last_error", "cx_version", "cx_set_blocks", "cx_set_veff", "cx_set_psi",
            "cx_get_psi", "cx_hpsi", "cx_chebyshev_filter", "cx_eigsolver", "cx_eigsolver_host", "cx_poisson", "cx_sync",
            "cx_timer_start", "cx_timer_stop", "cx_profile_stencil", "cx_profile_read", "cx_launch_count",
-           "cx_host_register", "cx_host_unregister", "cx_hpsi_noalloc", "cx_profile_read_apply", "cx_eig_fallback_count", "cx_scf", "cx_refine_eigenvalues", "cx_set_device"]
+           "cx_host_register", "cx_host_unregister", "cx_hpsi_noalloc", "cx_profile_read_apply", "cx_eig_fallback_count", "cx_scf", "cx_refine_eigenvalues", "cx_set_device",
+           "cx_eigsolver_full", "cx_eigsolver_full_host", "cx_scf_init", "cx_scf_step", "cx_scf_finish",
+           "cx_eig_hermitian_count"]
 
 
 class cx_grid(C.Structure):
@@ -53,6 +55,16 @@ class cx_scf_params(C.Structure):
 class cx_scf_result(C.Structure):
     _fields_ = [("Etotal", C.c_double), ("lambda_f", C.c_double), ("err", C.c_double), ("n_scf", C.c_int32),
                 ("converged", C.c_int32)]
+
+
+class cx_eig_params(C.Structure):
+    _fields_ = [("npl", C.c_int32), ("rhoTrigger", C.c_int32), ("elecgs_Count", C.c_int32), ("chefsibound_flag", C.c_int32)]
+
+
+class cx_scf_step_info(C.Structure):
+    _fields_ = [("Etotal", C.c_double), ("lambda_f", C.c_double), ("err", C.c_double), ("count", C.c_int32),
+                ("n_scf", C.c_int32), ("density_updated", C.c_int32), ("converged", C.c_int32),
+                ("poisson_iters", C.c_int32), ("pad", C.c_int32), ("step_ms", C.c_double), ("poisson_ms", C.c_double)]
 
 
 class cx_block(C.Structure):
@@ -90,6 +102,8 @@ def load(build_if_missing: bool = True):
                                 C.c_int32),
         "cx_eigsolver": ([h, C.c_int32, C.c_int32, C.c_int32, dp, dp, dp, dp], C.c_int32),
         "cx_eigsolver_host": ([h, C.c_int32, C.c_int32, C.c_int32, dp, dp, dp, dp, dp], C.c_int32),
+        "cx_eigsolver_full": ([h, P(cx_eig_params), C.c_int32, dp, dp, dp, dp, dp], C.c_int32),
+        "cx_eigsolver_full_host": ([h, P(cx_eig_params), C.c_int32, dp, dp, dp, dp, dp, dp], C.c_int32),
         "cx_poisson": ([h, dp, dp, C.c_double, C.c_int32, C.c_int32, P(C.c_int32), dp], C.c_int32),
         "cx_sync": ([h], C.c_int32),
         "cx_timer_start": ([h], C.c_int32),
@@ -102,8 +116,12 @@ def load(build_if_missing: bool = True):
         "cx_hpsi_noalloc": ([h, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32], C.c_int32),
         "cx_profile_read_apply": ([h, dp], C.c_int32),
         "cx_eig_fallback_count": ([h, P(C.c_int64)], C.c_int32),
+        "cx_eig_hermitian_count": ([h, P(C.c_int64)], C.c_int32),
         "cx_scf": ([h, P(cx_scf_params), dp, dp, dp, dp, P(cx_scf_result)], C.c_int32),
         "cx_refine_eigenvalues": ([h, dp], C.c_int32),
+        "cx_scf_init": ([h, P(cx_scf_params)], C.c_int32),
+        "cx_scf_step": ([h, dp, dp, P(cx_scf_step_info)], C.c_int32),
+        "cx_scf_finish": ([h, dp, dp, dp, P(cx_scf_result)], C.c_int32),
         "cx_set_device": ([C.c_int32], C.c_int32),
     }
     for name, (args, res) in sig.items():

@@ -38,6 +38,8 @@ cx_status build_maps(cx_handle h, const std::vector<const void*>& p0, const std:
 cx_status poisson_dev(cx_handle h, const double* d_f, double* d_phi, double tol, int32_t maxit, int32_t use_guess, int32_t* iters,
                       double* relres_out);
 cudaError_t launch_pinv_solve(double* io, int m, cudaStream_t st);
+// releases the SCF loop state (cx_scf.cu)
+void scf_state_free(cx_handle h);
 // FP64 Rayleigh quotients of the device-resident psi (cx_linalg.cu)
 cx_status refine_eigenvalues(cx_handle h, double* EigVal);
 // status flag of the TMA pipeline: CX_OK, or CX_ERR_CUDA with a message when a CTA timed out

@@ -12,6 +12,8 @@
 
 namespace cx {
 
+struct ScfState;                  // SCF run between cx_scf_init and cx_scf_finish (cx_scf.cu)
+
 constexpr int kMaxFDn = 8;
 
 // ---------------------------------------------------------------- complex helpers
@@ -180,6 +182,7 @@ struct cx_handle_s {
   void* d_misc = nullptr; size_t misc_bytes = 0;     // column norms, permutations, status
   void* d_pois = nullptr; size_t pois_bytes = 0;     // Poisson (AAR) vectors
   void* d_scf = nullptr; size_t scf_bytes = 0;       // SCF state (density, potentials, mixing history)
+  cx::ScfState* scf = nullptr;                       // loop state of the SCF run in progress
 
   // TMA path (complex64): float Veff, per-point projector entry start / count, tensor maps
   float* d_veff32 = nullptr;
@@ -199,6 +202,7 @@ struct cx_handle_s {
   int64_t launches = 0;
   int64_t eig_fallbacks = 0;                         // subspace eigensolves that needed the general solver
   int64_t eig_restarts = 0;                          // similarity restarts of the eigenvector refinement
+  int64_t eig_hermitian = 0;                         // subspace eigensolves answered by the Hermitian part
   int restart_fail_streak = 0;                       // blocks in a row whose restarts ended in the general solver
 };
 

@@ -178,6 +178,40 @@ __global__ void k_sylv_finish(const double2* __restrict__ EZ, const double2* __r
   }
 }
 
+// Gy <- D^-1/2 Gy D^-1/2 (unit diagonal) for the rotation check
+__global__ void k_unit_diag(double2* __restrict__ G, int n) {
+  const size_t tot = (size_t)n * n;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < tot; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = i % n, c = i / n;
+    const double d = sqrt(G[r * n + r].x * G[c * n + c].x);
+    if (r != c) G[i] = make_double2(G[i].x / d, G[i].y / d);
+  }
+}
+__global__ void k_unit_diag_fix(double2* __restrict__ G, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) G[(size_t)i * n + i] = make_double2(1.0, 0.0);
+}
+// smallest |R_jj| of a Cholesky factor (one CTA)
+__global__ void k_min_diag(const double2* __restrict__ R, int n, double* __restrict__ out) {
+  double m = 1e300;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double v = fabs(R[(size_t)i * n + i].x);
+    m = (v == v) ? fmin(m, v) : 0.0;
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
+  __shared__ double red[32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 1e300;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t = fmin(t, red[k]);
+    *out = t;
+  }
+}
+// eigenvalues of the Hermitian part (real) as complex values
+__global__ void k_real_to_complex(const double* __restrict__ a, double2* __restrict__ b, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = make_double2(a[i], 0.0);
+}
+
 // ------------------------------------------------------------------ batched Lanczos (W inner product)
 // Per block b the vectors live at v + b*N etc.; scalars alpha[j*nblk+b], beta2[j*nblk+b].
 __device__ __forceinline__ uint32_t hash32(uint32_t x) {
@@ -315,26 +349,145 @@ __global__ void k_tridiag_extremes(const double* __restrict__ alpha, const doubl
   lmax[blk] = 0.5 * (l + u);
 }
 
-// Batched Lanczos over all blocks: fills lmin/lmax (host, nblk each).
+// Replay of one Lanczos step with the scalars of the first pass (no reductions), accumulating the
+// Ritz vector: y += s_j v ; t = w - alpha_j v - beta_j vprev ; vprev = v ; v = t / beta_{j+1}
 template <typename R>
-static cx_status lanczos_bounds(cx_handle h, int K, std::vector<double>& lmin, std::vector<double>& lmax) {
+__global__ void k_lz_replay(const cplx<R>* __restrict__ w, cplx<R>* __restrict__ v, cplx<R>* __restrict__ vprev,
+                            double2* __restrict__ y, int N, const double* __restrict__ s_j, const double* __restrict__ alpha,
+                            const double* __restrict__ beta2, const double* __restrict__ beta2_next) {
+  const int b = blockIdx.y;
+  const double al = alpha[b];
+  const double be = beta2 ? sqrt(fmax(beta2[b], 0.0)) : 0.0;
+  const double bb = beta2_next[b];
+  const double inv = bb > 1e-200 ? 1.0 / sqrt(bb) : 0.0;
+  const double sj = s_j[b];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    const size_t k = (size_t)b * N + i;
+    const cplx<R> x = v[k], xp = vprev[k], ww = w[k];
+    y[k].x += sj * (double)x.x;
+    y[k].y += sj * (double)x.y;
+    cplx<R> t;
+    t.x = (R)((double)ww.x - al * x.x - be * xp.x);
+    t.y = (R)((double)ww.y - al * x.y - be * xp.y);
+    vprev[k] = x;
+    t.x = (R)(t.x * inv);
+    t.y = (R)(t.y * inv);
+    v[k] = t;
+  }
+}
+// Euclidean squared norm of each block's column of y (complex128)
+__global__ void k_norm2_cols(const double2* __restrict__ y, int N, double* __restrict__ acc) {
+  const int b = blockIdx.y;
+  const double2* x = y + (size_t)b * N;
+  double s = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) s += x[i].x * x[i].x + x[i].y * x[i].y;
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ double red[32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k];
+    atomicAdd(acc + b, t);
+  }
+}
+__global__ void k_scale_cols(double2* __restrict__ y, int N, const double* __restrict__ n2) {
+  const int b = blockIdx.y;
+  const double inv = n2[b] > 0 ? 1.0 / sqrt(n2[b]) : 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    const size_t k = (size_t)b * N + i;
+    y[k].x *= inv;
+    y[k].y *= inv;
+  }
+}
+
+// Effective Krylov length of block blk: the iteration stops at a breakdown (beta ~ 0); the same
+// rule as k_tridiag_extremes.
+static int lanczos_length(const std::vector<double>& beta2, int K, int nblk, int blk) {
+  for (int j = 1; j < K; ++j)
+    if (!(beta2[(size_t)j * nblk + blk] > 1e-24)) return j;
+  return K;
+}
+
+// Eigenvector of the Ke x Ke Lanczos tridiagonal (diagonal alpha, squared off-diagonals beta2)
+// for its eigenvalue mu, by inverse iteration with a dense pivoted solve (Ke <= 64).
+static std::vector<double> tridiag_eigvec(const std::vector<double>& alpha, const std::vector<double>& beta2, int Ke, int nblk,
+                                          int blk, double mu) {
+  const double scale = std::max(1.0, std::fabs(mu));
+  std::vector<double> x(Ke, 1.0), A((size_t)Ke * Ke);
+  for (int it = 0; it < 4; ++it) {
+    std::fill(A.begin(), A.end(), 0.0);
+    for (int j = 0; j < Ke; ++j) {
+      A[(size_t)j * Ke + j] = alpha[(size_t)j * nblk + blk] - mu;
+      if (j > 0) {
+        const double e = std::sqrt(std::max(0.0, beta2[(size_t)j * nblk + blk]));
+        A[(size_t)j * Ke + j - 1] = e;
+        A[(size_t)(j - 1) * Ke + j] = e;
+      }
+    }
+    std::vector<double> b = x;
+    // Gaussian elimination with partial pivoting (row-major A)
+    for (int c = 0; c < Ke; ++c) {
+      int p = c;
+      for (int r = c + 1; r < Ke; ++r)
+        if (std::fabs(A[(size_t)r * Ke + c]) > std::fabs(A[(size_t)p * Ke + c])) p = r;
+      if (p != c) {
+        for (int k = 0; k < Ke; ++k) std::swap(A[(size_t)p * Ke + k], A[(size_t)c * Ke + k]);
+        std::swap(b[p], b[c]);
+      }
+      double piv = A[(size_t)c * Ke + c];
+      if (std::fabs(piv) < 1e-14 * scale) piv = A[(size_t)c * Ke + c] = 1e-14 * scale;   // (near-)singular: the shift is an eigenvalue
+      for (int r = c + 1; r < Ke; ++r) {
+        const double f = A[(size_t)r * Ke + c] / piv;
+        if (f == 0.0) continue;
+        for (int k = c; k < Ke; ++k) A[(size_t)r * Ke + k] -= f * A[(size_t)c * Ke + k];
+        b[r] -= f * b[c];
+      }
+    }
+    for (int c = Ke - 1; c >= 0; --c) {
+      double t = b[c];
+      for (int k = c + 1; k < Ke; ++k) t -= A[(size_t)c * Ke + k] * x[k];
+      x[c] = t / A[(size_t)c * Ke + c];
+    }
+    double n = 0;
+    for (double v : x) n += v * v;
+    n = std::sqrt(n);
+    if (!(n > 0) || !std::isfinite(n)) { std::fill(x.begin(), x.end(), 0.0); x[0] = 1.0; break; }
+    for (double& v : x) v /= n;
+  }
+  return x;
+}
+
+// Batched Lanczos over all blocks in the W inner product: fills lmin/lmax (host, nblk each).
+// ubgv_in (host N x nblk complex128, may be null): start vector of each block whose column is
+// not zero (the others start from the seeded random vector).  ubgv_out (may be null): the Ritz
+// vector of the largest Ritz value of each block, 2-norm normalised, from a second pass that
+// replays the recurrence with the first pass's scalars (no K x N vector storage).
+template <typename R>
+static cx_status lanczos_bounds(cx_handle h, int K, std::vector<double>& lmin, std::vector<double>& lmax, const double* ubgv_in,
+                                double* ubgv_out) {
   const int nblk = h->nblk, N = h->g.N;
   const size_t vec = (size_t)N * nblk * sizeof(cplx<R>);
+  const size_t yvec = ubgv_out ? (size_t)N * nblk * sizeof(double2) : 0;
   const int nseg = std::max(1, h->nl.nseg);
   const size_t cpb = (size_t)nblk * nseg * kAngMax * sizeof(cplx<R>);
-  const size_t sc = (size_t)(2 * (K + 1) * nblk + 2 * nblk) * sizeof(double);
-  const size_t need = 3 * vec + cpb + sc + nblk * sizeof(BlockDev<R>) + nblk * sizeof(int2) + sizeof(StepScalars) * nblk + 1024;
+  const size_t sc = (size_t)(2 * (K + 1) * nblk + 3 * nblk + K * nblk) * sizeof(double);
+  const size_t need = 3 * vec + yvec + cpb + sc + nblk * sizeof(BlockDev<R>) + nblk * sizeof(int2) + sizeof(StepScalars) * nblk + 2048;
   cx_status s = ensure(h, &h->d_lz, &h->lz_bytes, need);
   if (s != CX_OK) return s;
   char* p = (char*)h->d_lz;
   cplx<R>* v = (cplx<R>*)p; p += vec;
   cplx<R>* w = (cplx<R>*)p; p += vec;
   cplx<R>* vprev = (cplx<R>*)p; p += vec;
+  p = (char*)(((uintptr_t)p + 255) & ~(uintptr_t)255);
+  double2* y = (double2*)p; p += yvec;
   cplx<R>* cprime = (cplx<R>*)p; p += cpb;
   double* alpha = (double*)p; p += (size_t)(K + 1) * nblk * sizeof(double);
   double* beta2 = (double*)p; p += (size_t)(K + 1) * nblk * sizeof(double);
   double* dmin = (double*)p; p += nblk * sizeof(double);
   double* dmax = (double*)p; p += nblk * sizeof(double);
+  double* n2 = (double*)p; p += nblk * sizeof(double);
+  double* svec = (double*)p; p += (size_t)K * nblk * sizeof(double);
   p = (char*)(((uintptr_t)p + 255) & ~(uintptr_t)255);
   BlockDev<R>* d_blk = (BlockDev<R>*)p; p += nblk * sizeof(BlockDev<R>);
   int2* d_tab = (int2*)p; p += nblk * sizeof(int2);
@@ -354,11 +507,30 @@ static cx_status lanczos_bounds(cx_handle h, int K, std::vector<double>& lmin, s
   CX_TRY_CUDA(h, cudaMemsetAsync(alpha, 0, 2 * (K + 1) * nblk * sizeof(double), h->stream));
 
   const dim3 rg((unsigned)std::min(64, (N + 255) / 256), (unsigned)nblk);
-  k_lz_init<R><<<grid_for((size_t)N * nblk), 256, 0, h->stream>>>(v, vprev, N, nblk, 12345u);
-  // ||v0||_W^2 into beta2 row K (scratch), then normalise
-  k_lz_dot<R><<<rg, 256, 0, h->stream>>>(v, v, h->d_W, N, beta2 + (size_t)K * nblk);
-  k_lz_norm0<R><<<rg, 256, 0, h->stream>>>(v, N, beta2 + (size_t)K * nblk);
-  h->launches += 3;
+  // start vectors: seeded random, replaced by the caller's guess where its column is not zero
+  std::vector<char> guess(nblk, 0);
+  if (ubgv_in)
+    for (int b = 0; b < nblk; ++b) {
+      const double* col = ubgv_in + 2 * (size_t)N * b;
+      for (size_t i = 0; i < 2 * (size_t)N; ++i)
+        if (col[i] != 0.0) { guess[b] = 1; break; }
+    }
+  auto start_vectors = [&]() -> cx_status {
+    k_lz_init<R><<<grid_for((size_t)N * nblk), 256, 0, h->stream>>>(v, vprev, N, nblk, 12345u);
+    h->launches++;
+    for (int b = 0; b < nblk; ++b)
+      if (guess[b]) {
+        cx_status st = cx_host_to_dev(h, ubgv_in + 2 * (size_t)N * b, v + (size_t)b * N, N, sizeof(R) == 4 ? CX_PREC_MIXED : CX_PREC_FP64);
+        if (st != CX_OK) return st;
+      }
+    // ||v0||_W^2, then normalise
+    CX_TRY_CUDA(h, cudaMemsetAsync(n2, 0, nblk * sizeof(double), h->stream));
+    k_lz_dot<R><<<rg, 256, 0, h->stream>>>(v, v, h->d_W, N, n2);
+    k_lz_norm0<R><<<rg, 256, 0, h->stream>>>(v, N, n2);
+    h->launches += 2;
+    return CX_OK;
+  };
+  if ((s = start_vectors()) != CX_OK) return s;
   for (int j = 0; j < K; ++j) {
     // w = H v
     cx_status st = fused_step<R>(h, d_blk, d_sc, nblk, d_tab, nblk, 0, false, cprime, true, 0.0);
@@ -376,6 +548,34 @@ static cx_status lanczos_bounds(cx_handle h, int K, std::vector<double>& lmin, s
   lmax.resize(nblk);
   CX_TRY_CUDA(h, cudaMemcpyAsync(lmin.data(), dmin, nblk * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   CX_TRY_CUDA(h, cudaMemcpyAsync(lmax.data(), dmax, nblk * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CX_TRY_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (!ubgv_out) return CX_OK;
+
+  // ---- Ritz vector of lmax: eigenvector s of the tridiagonal (host), then y = sum_j s_j v_j
+  std::vector<double> ha((size_t)(K + 1) * nblk), hb((size_t)(K + 1) * nblk), hs((size_t)K * nblk, 0.0);
+  CX_TRY_CUDA(h, cudaMemcpy(ha.data(), alpha, ha.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  CX_TRY_CUDA(h, cudaMemcpy(hb.data(), beta2, hb.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int b = 0; b < nblk; ++b) {
+    const int Ke = lanczos_length(hb, K, nblk, b);
+    const std::vector<double> x = tridiag_eigvec(ha, hb, Ke, nblk, b, lmax[b]);
+    for (int j = 0; j < Ke; ++j) hs[(size_t)j * nblk + b] = x[j];
+  }
+  CX_TRY_CUDA(h, cudaMemcpyAsync(svec, hs.data(), hs.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CX_TRY_CUDA(h, cudaMemsetAsync(y, 0, yvec, h->stream));
+  if ((s = start_vectors()) != CX_OK) return s;
+  for (int j = 0; j < K; ++j) {
+    cx_status st = fused_step<R>(h, d_blk, d_sc, nblk, d_tab, nblk, 0, false, cprime, true, 0.0);
+    if (st != CX_OK) return st;
+    k_lz_replay<R><<<rg, 256, 0, h->stream>>>(w, v, vprev, y, N, svec + (size_t)j * nblk, alpha + (size_t)j * nblk,
+                                              j > 0 ? beta2 + (size_t)j * nblk : nullptr, beta2 + (size_t)(j + 1) * nblk);
+    h->launches++;
+  }
+  CX_TRY_CUDA(h, cudaMemsetAsync(n2, 0, nblk * sizeof(double), h->stream));
+  k_norm2_cols<<<rg, 256, 0, h->stream>>>(y, N, n2);
+  k_scale_cols<<<rg, 256, 0, h->stream>>>(y, N, n2);
+  h->launches += 2;
+  CX_TRY_CUDA(h, cudaGetLastError());
+  CX_TRY_CUDA(h, cudaMemcpyAsync(ubgv_out, y, yvec, cudaMemcpyDeviceToHost, h->stream));
   CX_TRY_CUDA(h, cudaStreamSynchronize(h->stream));
   return CX_OK;
 }
@@ -401,6 +601,8 @@ static cx_status lanczos_bounds(cx_handle h, int K, std::vector<double>& lmin, s
 constexpr int kRestarts = 4;      // similarity restarts of a stalled refinement before the general solver
 constexpr int kRestartGiveUp = 4; // blocks in a row that needed the general solver after restarts: stop
                                   // restarting for the rest of the eigSolver call
+constexpr int kGeevMax = 512;     // largest block for the general FP64 solver (about 1 s at n = 1000)
+constexpr double kRotMinDiag = 1e-3;   // smallest Cholesky diagonal of the rotated block's unit-diagonal W-Gram
 
 struct RRWork {
   double2 *G, *Hs, *V, *ev;
@@ -412,11 +614,13 @@ struct RRWork {
   int* info;
   double2* Zbest;            // best iterate of a stalled refinement (restart point)
   int64_t* ipiv;             // LU pivots of a restart
+  double2* T0;               // the W-similar matrix T, kept for the Hermitian-part eigenpairs
+  double* rmin;              // smallest Cholesky diagonal of the rotation check
 };
 
 static cx_status rr_workspace(cx_handle h, int nmax, int ncolmax, RRWork& w) {
   const size_t n2 = (size_t)nmax * nmax;
-  const size_t need = n2 * 16 * 12 + nmax * 16 + nmax * 8 + 64 + n2 * 8 * 3 + (size_t)ncolmax * 8 + nmax * 4 + 64 + nmax * 8 + 40 * 256;
+  const size_t need = n2 * 16 * 13 + nmax * 16 + nmax * 8 + 64 + n2 * 8 * 3 + (size_t)ncolmax * 8 + nmax * 4 + 64 + nmax * 8 + 64 + 44 * 256;
   cx_status s = ensure(h, &h->d_rr, &h->rr_bytes, need);
   if (s != CX_OK) return s;
   char* p = (char*)h->d_rr;
@@ -443,6 +647,8 @@ static cx_status rr_workspace(cx_handle h, int nmax, int ncolmax, RRWork& w) {
   w.info = (int*)take(64);
   w.Zbest = (double2*)take(n2 * 16);
   w.ipiv = (int64_t*)take((size_t)nmax * 8);
+  w.T0 = (double2*)take(n2 * 16);
+  w.rmin = (double*)take(64);
   return CX_OK;
 }
 
@@ -529,13 +735,21 @@ cx_status rr_rotate<float>(cx_handle h, const float2* X, float2* out, int N, int
 // T X = X Lambda with X = I + Z directly; tier 2 starts it from the Hermitian eigenvectors U of
 // (T + T^H)/2 (B = U^H T U); c = U_w^-1 (U) X.  When neither converges (clustered spectrum, first
 // steps) the general solver cusolverDnXgeev runs on Hs = R A R^-1 (R = chol(G) in w.G) and
-// c = R^-1 v.  Returns in *used_fallback whether geev ran.
-static cx_status subspace_eig(cx_handle h, int n, RRWork& w, bool* used_fallback) {
+// c = R^-1 v, for blocks of at most kGeevMax states.
+// Every result must leave the rotated block well conditioned: the W-Gram of X c is Y^H Y with
+// Y = U_w c (the eigenvectors of T), and its unit-diagonal Cholesky factor must keep every
+// diagonal entry above kRotMinDiag.  A fixed point can converge to a degenerate solution (several
+// columns on one eigenvector) and a non-normal T can give nearly parallel general eigenvectors;
+// either is rejected.  The last resort is the Hermitian part itself: eigenvalues and eigenvectors
+// of (T + T^H)/2, whose real eigenvalues differ from the real parts of T's eigenvalues only at
+// second order in the anti-Hermitian part (its first-order term u^H T_a u is imaginary), with a
+// W-orthonormal rotation.  *path: 0 refinement, 1 general solver, 2 Hermitian part.
+static cx_status subspace_eig(cx_handle h, int n, RRWork& w, int* path) {
   const cuDoubleComplex one = make_cuDoubleComplex(1, 0), zero = make_cuDoubleComplex(0, 0);
   const size_t n2 = (size_t)n * n;
   const unsigned gn = grid_for(n2);
   cudaStream_t st = h->stream;
-  *used_fallback = false;
+  *path = 0;
   CX_TRY_BLAS(h, cublasSetMathMode(h->cublas, CUBLAS_DEFAULT_MATH));
   CX_TRY_CUDA(h, cudaMemcpyAsync(w.Hs0, w.Hs, n2 * 16, cudaMemcpyDeviceToDevice, st));
   // U_w = chol(Gw) (upper)
@@ -562,6 +776,43 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, bool* used_fallback
   CX_TRY_CUDA(h, cudaMemcpyAsync(&info, w.info, sizeof(int), cudaMemcpyDeviceToHost, st));
   CX_TRY_CUDA(h, cudaStreamSynchronize(st));
   bool fast = info == 0;
+  // is the block X c, c in w.V, well conditioned in the W inner product?  (w.EZ, w.B are scratch)
+  auto rotation_ok = [&](bool* ok) -> cx_status {
+    *ok = false;
+    CX_TRY_BLAS(h, cublasZtrmm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
+                               (const cuDoubleComplex*)w.Gw, n, (const cuDoubleComplex*)w.V, n, (cuDoubleComplex*)w.EZ, n));
+    CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_C, CUBLAS_OP_N, n, n, n, &one, (const cuDoubleComplex*)w.EZ, n,
+                               (const cuDoubleComplex*)w.EZ, n, &zero, (cuDoubleComplex*)w.B, n));
+    k_unit_diag<<<gn, 256, 0, st>>>(w.B, n);
+    k_unit_diag_fix<<<(n + 255) / 256, 256, 0, st>>>(w.B, n);
+    h->launches += 2;
+    CX_TRY_SOLVER(h, cusolverDnXpotrf(h->cusolver, h->cusolver_params, CUBLAS_FILL_MODE_UPPER, n, CUDA_C_64F, w.B, n, CUDA_C_64F,
+                                       h->d_ws, h->ws_bytes, h->h_ws, h->hws_bytes, w.info));
+    k_min_diag<<<1, 256, 0, st>>>(w.B, n, w.rmin);
+    h->launches++;
+    int inf = 0;
+    double rmin = 0;
+    CX_TRY_CUDA(h, cudaMemcpyAsync(&inf, w.info, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CX_TRY_CUDA(h, cudaMemcpyAsync(&rmin, w.rmin, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CX_TRY_CUDA(h, cudaStreamSynchronize(st));
+    *ok = inf == 0 && rmin > kRotMinDiag;
+    return CX_OK;
+  };
+  bool have_herm = false;     // w.U / w.wh hold the eigenpairs of (T + T^H)/2
+  auto hermitian_eig = [&]() -> cx_status {
+    k_herm_part<<<gn, 256, 0, st>>>(w.T0, w.U, n);
+    h->launches++;
+    CX_TRY_SOLVER(h, cusolverDnXsyevd(h->cusolver, h->cusolver_params, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, CUDA_C_64F,
+                                       w.U, n, CUDA_R_64F, w.wh, CUDA_C_64F, h->d_ws, h->ws_bytes, h->h_ws, h->hws_bytes, w.info));
+    CX_TRY_CUDA(h, cudaMemcpyAsync(&info, w.info, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CX_TRY_CUDA(h, cudaStreamSynchronize(st));
+    if (info != 0) {
+      h->err = "eigensolver: Hermitian eigensolver failed (info " + std::to_string(info) + ")";
+      return CX_ERR_LIB;
+    }
+    have_herm = true;
+    return CX_OK;
+  };
   // fixed-point refinement of B X = X Lambda (B in w.B is split in place into diag -> w.ev, off-diag);
   // returns true when converged, with lambda in w.ev and X = I + Z in w.Z
   // The mixed path runs the first sweeps with the B Z product on the tensor cores (complex64
@@ -629,6 +880,7 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, bool* used_fallback
                                (const cuDoubleComplex*)w.Gw, n, (const cuDoubleComplex*)w.Hs, n, (cuDoubleComplex*)w.T, n));
     CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
                                (const cuDoubleComplex*)w.Gw, n, (cuDoubleComplex*)w.T, n));
+    CX_TRY_CUDA(h, cudaMemcpyAsync(w.T0, w.T, n2 * 16, cudaMemcpyDeviceToDevice, st));
     // tier 1: the filtered block is ordered like the previous Ritz vectors, so near self-consistency T
     // itself is nearly diagonal -- refine directly (U = I)
     CX_TRY_CUDA(h, cudaMemcpyAsync(w.B, w.T, n2 * 16, cudaMemcpyDeviceToDevice, st));
@@ -640,24 +892,24 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, bool* used_fallback
       CX_TRY_CUDA(h, cudaMemcpyAsync(w.V, w.Z, n2 * 16, cudaMemcpyDeviceToDevice, st));
       CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
                                  (const cuDoubleComplex*)w.Gw, n, (cuDoubleComplex*)w.V, n));
-      return CX_OK;
+      bool ok = false;
+      if ((rs = rotation_ok(&ok)) != CX_OK) return rs;
+      if (ok) return CX_OK;
     }
-    // tier 2: Hermitian eigenvectors U of (T + T^H)/2, then refine B = U^H T U
-    k_herm_part<<<gn, 256, 0, st>>>(w.T, w.U, n);
-    h->launches++;
-    CX_TRY_SOLVER(h, cusolverDnXsyevd(h->cusolver, h->cusolver_params, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, CUDA_C_64F,
-                                       w.U, n, CUDA_R_64F, w.wh, CUDA_C_64F, h->d_ws, h->ws_bytes, h->h_ws, h->hws_bytes, w.info));
-    CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, (const cuDoubleComplex*)w.T, n,
+    // tier 2: Hermitian eigenvectors U of (T + T^H)/2, then refine B = U^H T U (blocks of more than
+    // kGeevMax states go to the Hermitian part directly: their refinement does not converge while
+    // the top of the block is unconverged, and its sweeps cost O(n^3) each)
+    if ((rs = hermitian_eig()) != CX_OK) return rs;
+    if (n > kGeevMax) goto hermitian_part;
+    CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, (const cuDoubleComplex*)w.T0, n,
                                (const cuDoubleComplex*)w.U, n, &zero, (cuDoubleComplex*)w.EZ, n));
     CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_C, CUBLAS_OP_N, n, n, n, &one, (const cuDoubleComplex*)w.U, n,
                                (const cuDoubleComplex*)w.EZ, n, &zero, (cuDoubleComplex*)w.B, n));
-    CX_TRY_CUDA(h, cudaMemcpyAsync(&info, w.info, sizeof(int), cudaMemcpyDeviceToHost, st));
-    CX_TRY_CUDA(h, cudaStreamSynchronize(st));
-    if (info == 0) {
+    {
       // B X = X Lambda by the fixed point; when it stalls, restart from the similar matrix
       // X^-1 B X with X = I + Z of the best iterate (each restart shrinks the coupling
-      // quadratically), accumulating the transforms in Xt (w.V, starting at U).  Bfull (w.T; T is
-      // no longer needed) keeps the matrix of the current round, since refine() splits w.B.
+      // quadratically), accumulating the transforms in Xt (w.V, starting at U).  Bfull (w.T)
+      // keeps the matrix of the current round, since refine() splits w.B.
       CX_TRY_CUDA(h, cudaMemcpyAsync(w.T, w.B, n2 * 16, cudaMemcpyDeviceToDevice, st));
       CX_TRY_CUDA(h, cudaMemcpyAsync(w.V, w.U, n2 * 16, cudaMemcpyDeviceToDevice, st));
       const int max_round = h->restart_fail_streak >= kRestartGiveUp ? 0 : kRestarts;
@@ -671,9 +923,14 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, bool* used_fallback
           CX_TRY_CUDA(h, cudaMemcpyAsync(w.V, w.Hs, n2 * 16, cudaMemcpyDeviceToDevice, st));
           CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n,
                                      &one, (const cuDoubleComplex*)w.Gw, n, (cuDoubleComplex*)w.V, n));
-          h->eig_restarts += round;
-          if (round > 0) h->restart_fail_streak = 0;
-          return CX_OK;
+          bool ok = false;
+          if ((rs = rotation_ok(&ok)) != CX_OK) return rs;
+          if (ok) {
+            h->eig_restarts += round;
+            if (round > 0) h->restart_fail_streak = 0;
+            return CX_OK;
+          }
+          break;                                                // degenerate fixed point
         }
         if (round == max_round || !(best_dm < 1.0)) {
           if (round > 0) h->restart_fail_streak++;
@@ -713,36 +970,55 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, bool* used_fallback
       }
     }
   }
-  // general FP64 eigensolver on Hs = R A R^-1 (the reference's matrix, better conditioned than A)
-  *used_fallback = true;
-  CX_TRY_BLAS(h, cublasZtrmm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
-                             (const cuDoubleComplex*)w.G, n, (const cuDoubleComplex*)w.Hs0, n, (cuDoubleComplex*)w.Hs, n));
-  CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
-                             (const cuDoubleComplex*)w.G, n, (cuDoubleComplex*)w.Hs, n));
-  size_t g1 = 0, g2 = 0;
-  CX_TRY_SOLVER(h, cusolverDnXgeev_bufferSize(h->cusolver, h->cusolver_params, CUSOLVER_EIG_MODE_NOVECTOR, CUSOLVER_EIG_MODE_VECTOR, n,
-                                               CUDA_C_64F, w.Hs, n, CUDA_C_64F, w.ev, CUDA_C_64F, nullptr, n, CUDA_C_64F, w.V, n,
-                                               CUDA_C_64F, &g1, &g2));
-  if ((s = ensure(h, &h->d_ws, &h->ws_bytes, g1 + 256)) != CX_OK) return s;
-  if (h->hws_bytes < g2 + 256) {
-    cudaFreeHost(h->h_ws);
-    h->h_ws = nullptr;
-    h->hws_bytes = 0;
-    CX_TRY_CUDA(h, cudaMallocHost(&h->h_ws, g2 + 256));
-    h->hws_bytes = g2 + 256;
+  if (!fast || n <= kGeevMax) {
+    // general FP64 eigensolver on Hs = R A R^-1 (the reference's matrix, better conditioned than A)
+    *path = 1;
+    CX_TRY_BLAS(h, cublasZtrmm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
+                               (const cuDoubleComplex*)w.G, n, (const cuDoubleComplex*)w.Hs0, n, (cuDoubleComplex*)w.Hs, n));
+    CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
+                               (const cuDoubleComplex*)w.G, n, (cuDoubleComplex*)w.Hs, n));
+    size_t g1 = 0, g2 = 0;
+    CX_TRY_SOLVER(h, cusolverDnXgeev_bufferSize(h->cusolver, h->cusolver_params, CUSOLVER_EIG_MODE_NOVECTOR, CUSOLVER_EIG_MODE_VECTOR, n,
+                                                 CUDA_C_64F, w.Hs, n, CUDA_C_64F, w.ev, CUDA_C_64F, nullptr, n, CUDA_C_64F, w.V, n,
+                                                 CUDA_C_64F, &g1, &g2));
+    if ((s = ensure(h, &h->d_ws, &h->ws_bytes, g1 + 256)) != CX_OK) return s;
+    if (h->hws_bytes < g2 + 256) {
+      cudaFreeHost(h->h_ws);
+      h->h_ws = nullptr;
+      h->hws_bytes = 0;
+      CX_TRY_CUDA(h, cudaMallocHost(&h->h_ws, g2 + 256));
+      h->hws_bytes = g2 + 256;
+    }
+    CX_TRY_SOLVER(h, cusolverDnXgeev(h->cusolver, h->cusolver_params, CUSOLVER_EIG_MODE_NOVECTOR, CUSOLVER_EIG_MODE_VECTOR, n,
+                                      CUDA_C_64F, w.Hs, n, CUDA_C_64F, w.ev, CUDA_C_64F, nullptr, n, CUDA_C_64F, w.V, n, CUDA_C_64F,
+                                      h->d_ws, h->ws_bytes, h->h_ws, h->hws_bytes, w.info));
+    CX_TRY_CUDA(h, cudaMemcpyAsync(&info, w.info, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CX_TRY_CUDA(h, cudaStreamSynchronize(st));
+    if (info != 0) {
+      h->err = "eigensolver: geev failed (info " + std::to_string(info) + ")";
+      return CX_ERR_LIB;
+    }
+    // rotation coefficients c = R^-1 v
+    CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
+                               (const cuDoubleComplex*)w.G, n, (cuDoubleComplex*)w.V, n));
+    if (!fast) return CX_OK;                                   // (no W-Cholesky factor to check against)
+    bool ok = false;
+    cx_status rs = rotation_ok(&ok);
+    if (rs != CX_OK) return rs;
+    if (ok) return CX_OK;
   }
-  CX_TRY_SOLVER(h, cusolverDnXgeev(h->cusolver, h->cusolver_params, CUSOLVER_EIG_MODE_NOVECTOR, CUSOLVER_EIG_MODE_VECTOR, n, CUDA_C_64F,
-                                    w.Hs, n, CUDA_C_64F, w.ev, CUDA_C_64F, nullptr, n, CUDA_C_64F, w.V, n, CUDA_C_64F, h->d_ws,
-                                    h->ws_bytes, h->h_ws, h->hws_bytes, w.info));
-  CX_TRY_CUDA(h, cudaMemcpyAsync(&info, w.info, sizeof(int), cudaMemcpyDeviceToHost, st));
-  CX_TRY_CUDA(h, cudaStreamSynchronize(st));
-  if (info != 0) {
-    h->err = "eigensolver: geev failed (info " + std::to_string(info) + ")";
-    return CX_ERR_LIB;
+  // Hermitian part: eigenvalues wh (real), c = U_w^-1 U
+hermitian_part:
+  *path = 2;
+  if (!have_herm) {
+    cx_status rs = hermitian_eig();
+    if (rs != CX_OK) return rs;
   }
-  // rotation coefficients c = R^-1 v
+  k_real_to_complex<<<(n + 255) / 256, 256, 0, st>>>(w.wh, w.ev, n);
+  h->launches++;
+  CX_TRY_CUDA(h, cudaMemcpyAsync(w.V, w.U, n2 * 16, cudaMemcpyDeviceToDevice, st));
   CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
-                             (const cuDoubleComplex*)w.G, n, (cuDoubleComplex*)w.V, n));
+                             (const cuDoubleComplex*)w.Gw, n, (cuDoubleComplex*)w.V, n));
   return CX_OK;
 }
 
@@ -789,9 +1065,10 @@ static cx_status rayleigh_ritz_block(cx_handle h, int b, int sel, RRWork& w, dou
   CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
                              (const cuDoubleComplex*)w.G, n, (cuDoubleComplex*)w.Hs, n));
   // eigenpairs of Hs (general; eigSolver.m:110 -- Hs is not Hermitian for Cyclix cells)
-  bool fb = false;
-  if ((s = subspace_eig(h, n, w, &fb)) != CX_OK) return s;
-  h->eig_fallbacks += fb ? 1 : 0;
+  int path = 0;
+  if ((s = subspace_eig(h, n, w, &path)) != CX_OK) return s;
+  h->eig_fallbacks += path == 1 ? 1 : 0;
+  h->eig_hermitian += path == 2 ? 1 : 0;
   std::vector<std::complex<double>> ev(n);
   CX_TRY_CUDA(h, cudaMemcpyAsync(ev.data(), w.ev, n * 16, cudaMemcpyDeviceToHost, h->stream));
   CX_TRY_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -816,26 +1093,43 @@ static cx_status rayleigh_ritz_block(cx_handle h, int b, int sel, RRWork& w, dou
 }
 
 template <typename R>
-static cx_status eigsolver_T(cx_handle h, int count, int npl, int rhoTrigger, double* EigVal, double* a0, double* bup, double* lc) {
-  const int nblk = h->nblk;
+static cx_status eigsolver_T(cx_handle h, const cx_eig_params& P, int count, double* ubgv, double* EigVal, double* a0, double* bup,
+                             double* lc) {
+  const int nblk = h->nblk, npl = P.npl;
+  // subsequent relaxation steps filter with the current bounds from the first SCF cycle on
+  // (src/eigSolver.m:21-23)
+  const int elecgs = P.elecgs_Count < 1 ? 1 : P.elecgs_Count;
+  const int rhoTrigger = elecgs > 1 ? 1 : P.rhoTrigger;
   h->restart_fail_streak = 0;
   std::vector<int> off(nblk + 1, 0);
   for (int b = 0; b < nblk; ++b) off[b + 1] = off[b] + h->blocks[b].Ns;
-  // ---- bounds and cutoff (eigSolver.m:47-94, first relaxation step)
+  auto min_ev = [&](int b) { return *std::min_element(EigVal + off[b], EigVal + off[b + 1]); };
+  auto max_ev = [&](int b) { return *std::max_element(EigVal + off[b], EigVal + off[b + 1]); };
+  // ---- bounds (src/eigSolver.m:47-84).  The upper bound is 1.01 x the largest Ritz value of a
+  // Lanczos run; on the first relaxation step it starts from a random vector, later from the
+  // previous upper-bound vector ubgv, whose update is returned in ubgv.
+  const int K = 64;
   if (count == 1) {
     std::vector<double> lmin, lmax;
-    cx_status s = lanczos_bounds<R>(h, 64, lmin, lmax);
+    cx_status s = lanczos_bounds<R>(h, K, lmin, lmax, elecgs > 1 ? ubgv : nullptr, ubgv);
     if (s != CX_OK) return s;
     for (int b = 0; b < nblk; ++b) {
       bup[b] = lmax[b] * 1.01;
-      a0[b] = lmin[b] - 0.1;
+      a0[b] = elecgs == 1 ? lmin[b] - 0.1 : min_ev(b);
     }
   } else if (count > rhoTrigger) {
-    for (int b = 0; b < nblk; ++b) a0[b] = *std::min_element(EigVal + off[b], EigVal + off[b + 1]);
+    if (P.chefsibound_flag == 1) {
+      std::vector<double> lmin, lmax;
+      cx_status s = lanczos_bounds<R>(h, K, lmin, lmax, ubgv, ubgv);
+      if (s != CX_OK) return s;
+      for (int b = 0; b < nblk; ++b) bup[b] = lmax[b] * 1.01;
+    }
+    for (int b = 0; b < nblk; ++b) a0[b] = min_ev(b);
   }
+  // ---- filter cutoff (src/eigSolver.m:88-94)
   std::vector<double> va(nblk), vb(nblk), va0(nblk);
   for (int b = 0; b < nblk; ++b) {
-    lc[b] = count == 1 ? 0.5 * (bup[b] + a0[b]) : *std::max_element(EigVal + off[b], EigVal + off[b + 1]) + 0.10;
+    lc[b] = (count == 1 && elecgs == 1) ? 0.5 * (bup[b] + a0[b]) : max_ev(b) + 0.10;
     va[b] = lc[b];
     vb[b] = bup[b];
     va0[b] = a0[b];
@@ -918,6 +1212,7 @@ cx_status cx_dev_to_host(cx_handle h, const void* dev, double* host, size_t n, i
 }
 
 void cx_free_extra(cx_handle h) {
+  cx::scf_state_free(h);
   cudaFree(h->d_stage); h->d_stage = nullptr;
   cudaFree(h->d_rr); h->d_rr = nullptr;
   cudaFree(h->d_lz); h->d_lz = nullptr;
@@ -1015,20 +1310,28 @@ cx_status refine_eigenvalues(cx_handle h, double* EigVal) {
 }
 
 cx_status eigsolver_dispatch(cx_handle h, int count, int npl, int rhoTrigger, double* EigVal, double* a0, double* bup, double* lc) {
-  if (h->prec == CX_PREC_FP64) return eigsolver_T<double>(h, count, npl, rhoTrigger, EigVal, a0, bup, lc);
-  return eigsolver_T<float>(h, count, npl, rhoTrigger, EigVal, a0, bup, lc);
+  const cx_eig_params P{npl, rhoTrigger, 1, 0};
+  if (h->prec == CX_PREC_FP64) return eigsolver_T<double>(h, P, count, nullptr, EigVal, a0, bup, lc);
+  return eigsolver_T<float>(h, P, count, nullptr, EigVal, a0, bup, lc);
 }
 }  // namespace cx
 
 extern "C" {
 
+cx_status cx_eigsolver_full(cx_handle h, const cx_eig_params* p, int32_t count, double* ubgv, double* EigVal, double* a0, double* bup,
+                            double* lambda_cutoff) {
+  if (!h) return CX_ERR_ARG;
+  if (!p || !EigVal || !a0 || !bup || !lambda_cutoff) { h->err = "cx_eigsolver: null argument"; return CX_ERR_ARG; }
+  if (h->nblk < 1) { h->err = "cx_eigsolver: call cx_set_blocks first"; return CX_ERR_STATE; }
+  if (count < 1 || p->npl < 1) { h->err = "cx_eigsolver: need count >= 1 and npl >= 1"; return CX_ERR_ARG; }
+  if (h->prec == CX_PREC_FP64) return eigsolver_T<double>(h, *p, count, ubgv, EigVal, a0, bup, lambda_cutoff);
+  return eigsolver_T<float>(h, *p, count, ubgv, EigVal, a0, bup, lambda_cutoff);
+}
+
 cx_status cx_eigsolver(cx_handle h, int32_t count, int32_t npl, int32_t rhoTrigger, double* EigVal, double* a0, double* bup,
                        double* lambda_cutoff) {
-  if (!h || !EigVal || !a0 || !bup || !lambda_cutoff) return CX_ERR_ARG;
-  if (h->nblk < 1) { h->err = "cx_eigsolver: call cx_set_blocks first"; return CX_ERR_STATE; }
-  if (count < 1 || npl < 1) { h->err = "cx_eigsolver: need count >= 1 and npl >= 1"; return CX_ERR_ARG; }
-  if (h->prec == CX_PREC_FP64) return eigsolver_T<double>(h, count, npl, rhoTrigger, EigVal, a0, bup, lambda_cutoff);
-  return eigsolver_T<float>(h, count, npl, rhoTrigger, EigVal, a0, bup, lambda_cutoff);
+  const cx_eig_params P{npl, rhoTrigger, 1, 0};
+  return cx_eigsolver_full(h, &P, count, nullptr, EigVal, a0, bup, lambda_cutoff);
 }
 
 cx_status cx_refine_eigenvalues(cx_handle h, double* EigVal) {
@@ -1043,9 +1346,16 @@ cx_status cx_eig_fallback_count(cx_handle h, int64_t* count) {
   return CX_OK;
 }
 
-cx_status cx_eigsolver_host(cx_handle h, int32_t count, int32_t npl, int32_t rhoTrigger, double* psi, double* EigVal, double* a0,
-                            double* bup, double* lambda_cutoff) {
-  if (!h || !psi) return CX_ERR_ARG;
+cx_status cx_eig_hermitian_count(cx_handle h, int64_t* count) {
+  if (!h || !count) return CX_ERR_ARG;
+  *count = h->eig_hermitian;
+  return CX_OK;
+}
+
+cx_status cx_eigsolver_full_host(cx_handle h, const cx_eig_params* p, int32_t count, double* ubgv, double* psi, double* EigVal,
+                                 double* a0, double* bup, double* lambda_cutoff) {
+  if (!h) return CX_ERR_ARG;
+  if (!psi) { h->err = "cx_eigsolver_host: null psi"; return CX_ERR_ARG; }
   if (h->nblk < 1) { h->err = "cx_eigsolver_host: call cx_set_blocks first"; return CX_ERR_STATE; }
   size_t off = 0;
   for (int b = 0; b < h->nblk; ++b) {
@@ -1053,7 +1363,7 @@ cx_status cx_eigsolver_host(cx_handle h, int32_t count, int32_t npl, int32_t rho
     if (s != CX_OK) return s;
     off += (size_t)h->g.N * h->blocks[b].Ns;
   }
-  cx_status s = cx_eigsolver(h, count, npl, rhoTrigger, EigVal, a0, bup, lambda_cutoff);
+  cx_status s = cx_eigsolver_full(h, p, count, ubgv, EigVal, a0, bup, lambda_cutoff);
   if (s != CX_OK) return s;
   off = 0;
   for (int b = 0; b < h->nblk; ++b) {
@@ -1062,6 +1372,12 @@ cx_status cx_eigsolver_host(cx_handle h, int32_t count, int32_t npl, int32_t rho
     off += (size_t)h->g.N * h->blocks[b].Ns;
   }
   return CX_OK;
+}
+
+cx_status cx_eigsolver_host(cx_handle h, int32_t count, int32_t npl, int32_t rhoTrigger, double* psi, double* EigVal, double* a0,
+                            double* bup, double* lambda_cutoff) {
+  const cx_eig_params P{npl, rhoTrigger, 1, 0};
+  return cx_eigsolver_full_host(h, &P, count, nullptr, psi, EigVal, a0, bup, lambda_cutoff);
 }
 
 }  // extern "C"

@@ -219,6 +219,28 @@ struct ScfBufs {
   int nred;
 };
 
+// State of an SCF run between cx_scf_init and cx_scf_finish (the loop variables of src/scf.m).
+struct ScfState {
+  cx_scf_params P{};
+  ScfBufs B{};
+  std::vector<double> wblk, ev, a0, bup, lc, hist;
+  double sums[kNSums] = {};
+  double ptol = 0, err = 100.0, Etot = 0.0, lam_f = 0.0;
+  int pmax = 1000, rhoTrigger = 4, count = 1, count_scf = 1;
+  cudaEvent_t e0 = nullptr, e1 = nullptr, p0 = nullptr, p1 = nullptr;
+  ~ScfState() {
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (p0) cudaEventDestroy(p0);
+    if (p1) cudaEventDestroy(p1);
+  }
+};
+
+void scf_state_free(cx_handle h) {
+  delete h->scf;
+  h->scf = nullptr;
+}
+
 template <typename R>
 static cx_status density_all(cx_handle h, const ScfBufs& B, const std::vector<double>& wblk) {
   const int N = h->g.N;
@@ -236,25 +258,77 @@ static cx_status density_all(cx_handle h, const ScfBufs& B, const std::vector<do
 
 cx_status eigsolver_dispatch(cx_handle h, int count, int npl, int rhoTrigger, double* EigVal, double* a0, double* bup, double* lc);
 
+static unsigned grid_n(int N) { return (unsigned)std::min(152 * 8, (N + 255) / 256); }
+
+// phi = Poisson(rho), Vxc(rho), Veff = phi + Vxc (into h->d_veff) and the energy / error sums
+static cx_status scf_potential(cx_handle h, ScfState& S, int use_guess, int* iters, float* pms) {
+  const int N = h->g.N;
+  const unsigned gN = grid_n(N);
+  const cudaStream_t st = h->stream;
+  ScfBufs& B = S.B;
+  k_poisson_rhs<<<gN, 256, 0, st>>>(B.rho, B.b, B.f, N);
+  h->launches++;
+  int it = 0;
+  double rr = 0;
+  CX_TRY_CUDA(h, cudaEventRecord(S.p0, st));
+  cx_status s = poisson_dev(h, B.f, B.phi, S.ptol, S.pmax, use_guess, &it, &rr);
+  if (s != CX_OK && s != CX_ERR_NOCONV) return s;
+  CX_TRY_CUDA(h, cudaEventRecord(S.p1, st));
+  k_xc_veff<<<gN, 256, 0, st>>>(B.rho, B.phi, B.b, h->d_W, B.vin, B.vxc, h->d_veff, N, B.partial);
+  k_sum_partials<<<1, 32 * kNSums, 0, st>>>(B.partial, (int)gN, kNSums, B.sums);
+  h->launches += 2;
+  CX_TRY_CUDA(h, cudaMemcpyAsync(S.sums, B.sums, sizeof(S.sums), cudaMemcpyDeviceToHost, st));
+  CX_TRY_CUDA(h, cudaStreamSynchronize(st));
+  if (iters) *iters = it;
+  if (pms) CX_TRY_CUDA(h, cudaEventElapsedTime(pms, S.p0, S.p1));
+  return CX_OK;
+}
+
+// the block operators read d_veff (complex128 path) and its float copy (complex64 path)
+static cx_status scf_refresh_veff(cx_handle h) {
+  if (h->d_veff32) {
+    k_to_float<<<grid_n(h->g.N), 256, 0, h->stream>>>(h->d_veff, h->d_veff32, h->g.N);
+    h->launches++;
+  }
+  CX_TRY_CUDA(h, cudaGetLastError());
+  return CX_OK;
+}
+
+static constexpr double kC2 = 0.73855876638202;
+
+static double total_energy(const ScfState& S, const double occout[3]) {
+  const double Exc = S.sums[0] - kC2 * S.sums[1], Exc_dc = S.sums[2], Eelec_dc = 0.5 * S.sums[3], Escc = S.sums[4];
+  return occout[1] + Exc - Exc_dc + Eelec_dc - S.P.Eself + S.P.E_corr + occout[2] + Escc;
+}
+
 }  // namespace cx
 
 using namespace cx;
 
-extern "C" cx_status cx_scf(cx_handle h, const cx_scf_params* P, double* EigVal, double* rho_out, double* Veff_out, double* hist,
-                            cx_scf_result* res) {
-  if (!h || !P || !EigVal || !res) return CX_ERR_ARG;
+extern "C" cx_status cx_scf_init(cx_handle h, const cx_scf_params* P) {
+  if (!h) return CX_ERR_ARG;
+  if (!P) { h->err = "cx_scf_init: null parameters"; return CX_ERR_ARG; }
   if (h->nblk < 1) { h->err = "cx_scf: call cx_set_blocks (and cx_set_psi) first"; return CX_ERR_STATE; }
   if (h->nspin != 1) { h->err = "cx_scf: the SCF driver supports nspin = 1 (spin blocks are supported by cx_eigsolver)"; return CX_ERR_ARG; }
   if (!P->b || !P->rho0 || !P->wkpt || P->max_scf < 1 || P->npl < 1 || !(P->scf_tol > 0) || !(P->bet > 0)) {
     h->err = "cx_scf: need b, rho0, wkpt, max_scf >= 1, npl >= 1, scf_tol > 0, bet > 0";
     return CX_ERR_ARG;
   }
+  scf_state_free(h);
+  ScfState* S = new ScfState();
+  h->scf = S;
+  S->P = *P;
+  S->P.b = S->P.rho0 = nullptr;              // read here only
   const int N = h->g.N, nblk = h->nblk, m = kMixHist;
   const cudaStream_t st = h->stream;
-  const unsigned gN = (unsigned)std::min(152 * 8, (N + 255) / 256);
+  const unsigned gN = grid_n(N);
   const int ntot = h->nstates;
+  CX_TRY_CUDA(h, cudaEventCreate(&S->e0));
+  CX_TRY_CUDA(h, cudaEventCreate(&S->e1));
+  CX_TRY_CUDA(h, cudaEventCreate(&S->p0));
+  CX_TRY_CUDA(h, cudaEventCreate(&S->p1));
   // ---- device buffers
-  ScfBufs B{};
+  ScfBufs& B = S->B;
   B.nred = (int)gN;
   const size_t need = (size_t)N * 8 * (9 + 2 * m) + (size_t)gN * kNSums * 8 + 64 * 8 + (size_t)ntot * 8 * 3 + 8 * (m * m + 2 * m + 8) +
                       64 * 256;
@@ -274,9 +348,10 @@ extern "C" cx_status cx_scf(cx_handle h, const cx_scf_params* P, double* EigVal,
     B.partial = take((size_t)gN * kNSums * 8); B.sums = take(64 * 8); B.ev = take((size_t)ntot * 8); B.occ = take((size_t)ntot * 8);
     B.wst = take((size_t)ntot * 8); B.occout = take(8 * 8); B.io = take(8 * (m * m + 2 * m + 8));
   }
-  std::vector<double> wblk(P->wkpt, P->wkpt + nblk), wst(ntot);
+  S->wblk.assign(P->wkpt, P->wkpt + nblk);
+  std::vector<double> wst(ntot);
   for (int b = 0, o = 0; b < nblk; ++b)
-    for (int j = 0; j < h->blocks[b].Ns; ++j) wst[o++] = wblk[b];
+    for (int j = 0; j < h->blocks[b].Ns; ++j) wst[o++] = S->wblk[b];
   CX_TRY_CUDA(h, cudaMemcpyAsync(B.wst, wst.data(), ntot * 8, cudaMemcpyHostToDevice, st));
   CX_TRY_CUDA(h, cudaMemcpyAsync(B.b, P->b, (size_t)N * 8, cudaMemcpyHostToDevice, st));
   CX_TRY_CUDA(h, cudaMemcpyAsync(B.rho, P->rho0, (size_t)N * 8, cudaMemcpyHostToDevice, st));
@@ -284,113 +359,161 @@ extern "C" cx_status cx_scf(cx_handle h, const cx_scf_params* P, double* EigVal,
   CX_TRY_CUDA(h, cudaMemsetAsync(B.F, 0, (size_t)N * 8 * m, st));
   CX_TRY_CUDA(h, cudaMemsetAsync(B.fkm1, 0, (size_t)N * 8, st));
   CX_TRY_CUDA(h, cudaMemsetAsync(B.vin, 0, (size_t)N * 8, st));
-  const double ptol = P->poisson_tol > 0 ? P->poisson_tol : 0.01 * P->scf_tol;
-  const int pmax = P->maxit_poisson > 0 ? P->maxit_poisson : 1000;
-  double sums[kNSums];
-  auto refresh_veff = [&]() -> cx_status {
-    // the block operators read d_veff (complex128 path) and its float copy (complex64 path)
-    if (h->d_veff32) {
-      k_to_float<<<gN, 256, 0, st>>>(h->d_veff, h->d_veff32, N);
-      h->launches++;
-    }
-    CX_TRY_CUDA(h, cudaGetLastError());
-    return CX_OK;
-  };
-  auto potential = [&](int use_guess) -> cx_status {
-    // phi = Poisson(rho), Vxc(rho), Veff = phi + Vxc (into h->d_veff) and the energy / error sums
-    k_poisson_rhs<<<gN, 256, 0, st>>>(B.rho, B.b, B.f, N);
-    h->launches++;
-    int it = 0;
-    double rr = 0;
-    cx_status s = poisson_dev(h, B.f, B.phi, ptol, pmax, use_guess, &it, &rr);
-    if (s != CX_OK && s != CX_ERR_NOCONV) return s;
-    k_xc_veff<<<gN, 256, 0, st>>>(B.rho, B.phi, B.b, h->d_W, B.vin, B.vxc, h->d_veff, N, B.partial);
-    k_sum_partials<<<1, 32 * kNSums, 0, st>>>(B.partial, (int)gN, kNSums, B.sums);
-    h->launches += 2;
-    CX_TRY_CUDA(h, cudaMemcpyAsync(sums, B.sums, sizeof(sums), cudaMemcpyDeviceToHost, st));
-    CX_TRY_CUDA(h, cudaStreamSynchronize(st));
-    return CX_OK;
-  };
+  S->ptol = P->poisson_tol > 0 ? P->poisson_tol : 0.01 * P->scf_tol;
+  S->pmax = P->maxit_poisson > 0 ? P->maxit_poisson : 1000;
+  S->rhoTrigger = P->rhoTrigger > 0 ? P->rhoTrigger : 4;
+  S->a0.assign(nblk, 0.0);
+  S->bup.assign(nblk, 0.0);
+  S->lc.assign(nblk, 0.0);
+  S->ev.assign(ntot, 0.0);
+  S->hist.clear();
+  S->count = 1;
+  S->count_scf = 1;
+  S->err = 100.0;
+  S->Etot = S->lam_f = 0.0;
   cx_status s;
   // ---- initial potential (src/scf.m:32-39)
-  if ((s = potential(0)) != CX_OK) return s;
-  if ((s = refresh_veff()) != CX_OK) return s;
+  if ((s = scf_potential(h, *S, 0, nullptr, nullptr)) != CX_OK) return s;
+  if ((s = scf_refresh_veff(h)) != CX_OK) return s;
   CX_TRY_CUDA(h, cudaMemcpyAsync(B.vin, h->d_veff, (size_t)N * 8, cudaMemcpyDeviceToDevice, st));   // Veff_temp
-  std::vector<double> a0(nblk, 0.0), bup(nblk, 0.0), lc(nblk, 0.0);
-  std::vector<double> ev(ntot, 0.0);
-  int count = 1, count_scf = 1;
-  double err = 100.0, Etot = 0.0, lam_f = 0.0;
-  const double C2 = 0.73855876638202;
-  const int rhoTrigger = P->rhoTrigger > 0 ? P->rhoTrigger : 4;
-  while ((err > P->scf_tol && count_scf <= P->max_scf) || count_scf <= P->min_scf) {
-    if ((s = eigsolver_dispatch(h, count, P->npl, rhoTrigger, ev.data(), a0.data(), bup.data(), lc.data())) != CX_OK) return s;
-    CX_TRY_CUDA(h, cudaMemcpyAsync(B.ev, ev.data(), ntot * 8, cudaMemcpyHostToDevice, st));
-    k_occupations<<<1, 1024, 0, st>>>(B.ev, B.wst, ntot, P->bet, P->occfac, P->NegCharge, P->elec_T_type == 0, B.occ, B.occout);
-    h->launches++;
-    double occout[3];
-    CX_TRY_CUDA(h, cudaMemcpyAsync(occout, B.occout, sizeof(occout), cudaMemcpyDeviceToHost, st));
-    CX_TRY_CUDA(h, cudaStreamSynchronize(st));
-    lam_f = occout[0];
-    if (count >= rhoTrigger) {
-      s = h->prec == CX_PREC_FP64 ? density_all<double>(h, B, wblk) : density_all<float>(h, B, wblk);
-      if (s != CX_OK) return s;
-      if ((s = potential(1)) != CX_OK) return s;
-      const double Exc = sums[0] - C2 * sums[1], Exc_dc = sums[2], Eelec_dc = 0.5 * sums[3], Escc = sums[4];
-      Etot = occout[1] + Exc - Exc_dc + Eelec_dc - P->Eself + P->E_corr + occout[2] + Escc;
-      err = std::sqrt(sums[5]) / std::sqrt(sums[6]);
-      if (hist && count_scf <= P->max_scf) {
-        hist[2 * (count_scf - 1)] = Etot / std::max(1, P->n_atm);
-        hist[2 * (count_scf - 1) + 1] = err;
-      }
-      if (err > P->scf_tol || count_scf < P->min_scf) {
-        // potential mixing of the mean-free Veff (the mean is 0 for non-periodic cells, src/scf.m:201-215)
-        const int col = (count_scf - 2 + m) % m;
-        k_mix_hist<<<gN, 256, 0, st>>>(h->d_veff, B.vin, B.fk, B.X, B.F, B.xkm1, B.fkm1, N, col, count_scf > 1 ? 1 : 0);
-        h->launches++;
-        const int anderson = count_scf > 1 ? 1 : 0;     // PulayFrequency = 1
-        if (anderson) {
-          k_mix_gram<<<m * (m + 1), 256, 0, st>>>(B.F, B.fk, N, m, B.io);
-          CX_TRY_CUDA(h, launch_pinv_solve(B.io, m, st));
-          h->launches += 2;
-        }
-        k_mix_update<<<gN, 256, 0, st>>>(B.X, B.F, B.io + m * m + m, anderson, P->mixing_param > 0 ? P->mixing_param : 0.3, B.vin, B.fk,
-                                         B.xkm1, B.fkm1, h->d_veff, N, m);
-        h->launches++;
-        CX_TRY_CUDA(h, cudaMemcpyAsync(B.vin, h->d_veff, (size_t)N * 8, cudaMemcpyDeviceToDevice, st));
-      }
-      if ((s = refresh_veff()) != CX_OK) return s;
-      count_scf++;
-    }
-    count++;
-    if (count > 10 * (P->max_scf + rhoTrigger)) break;
-  }
   CX_TRY_CUDA(h, cudaStreamSynchronize(st));
-  if (P->refine && count_scf > 1) {
+  return CX_OK;
+}
+
+extern "C" cx_status cx_scf_step(cx_handle h, double* psi_host, double* EigVal, cx_scf_step_info* info) {
+  if (!h) return CX_ERR_ARG;
+  if (!h->scf) { h->err = "cx_scf_step: call cx_scf_init first"; return CX_ERR_STATE; }
+  ScfState& S = *h->scf;
+  ScfBufs& B = S.B;
+  const int N = h->g.N, m = kMixHist, ntot = h->nstates;
+  const unsigned gN = grid_n(N);
+  const cudaStream_t st = h->stream;
+  const cx_scf_params& P = S.P;
+  cx_status s;
+  cx_scf_step_info out{};
+  // the caller's psi (S.psi on the host): copied in before the step and out after it
+  if (psi_host) {
+    size_t off = 0;
+    for (int b = 0; b < h->nblk; ++b) {
+      if ((s = cx_set_psi(h, b, psi_host + 2 * off)) != CX_OK) return s;
+      off += (size_t)N * h->blocks[b].Ns;
+    }
+  }
+  CX_TRY_CUDA(h, cudaEventRecord(S.e0, st));
+  if ((s = eigsolver_dispatch(h, S.count, P.npl, S.rhoTrigger, S.ev.data(), S.a0.data(), S.bup.data(), S.lc.data())) != CX_OK) return s;
+  CX_TRY_CUDA(h, cudaMemcpyAsync(B.ev, S.ev.data(), ntot * 8, cudaMemcpyHostToDevice, st));
+  k_occupations<<<1, 1024, 0, st>>>(B.ev, B.wst, ntot, P.bet, P.occfac, P.NegCharge, P.elec_T_type == 0, B.occ, B.occout);
+  h->launches++;
+  double occout[3];
+  CX_TRY_CUDA(h, cudaMemcpyAsync(occout, B.occout, sizeof(occout), cudaMemcpyDeviceToHost, st));
+  CX_TRY_CUDA(h, cudaStreamSynchronize(st));
+  S.lam_f = occout[0];
+  if (S.count >= S.rhoTrigger) {
+    s = h->prec == CX_PREC_FP64 ? density_all<double>(h, B, S.wblk) : density_all<float>(h, B, S.wblk);
+    if (s != CX_OK) return s;
+    float pms = 0;
+    if ((s = scf_potential(h, S, 1, &out.poisson_iters, &pms)) != CX_OK) return s;
+    out.poisson_ms = pms;
+    S.Etot = total_energy(S, occout);
+    S.err = std::sqrt(S.sums[5]) / std::sqrt(S.sums[6]);
+    S.hist.push_back(S.Etot / std::max(1, P.n_atm));
+    S.hist.push_back(S.err);
+    if (S.err > P.scf_tol || S.count_scf < P.min_scf) {
+      // potential mixing of the mean-free Veff (the mean is 0 for non-periodic cells, src/scf.m:201-215)
+      const int col = (S.count_scf - 2 + m) % m;
+      k_mix_hist<<<gN, 256, 0, st>>>(h->d_veff, B.vin, B.fk, B.X, B.F, B.xkm1, B.fkm1, N, col, S.count_scf > 1 ? 1 : 0);
+      h->launches++;
+      const int anderson = S.count_scf > 1 ? 1 : 0;     // PulayFrequency = 1
+      if (anderson) {
+        k_mix_gram<<<m * (m + 1), 256, 0, st>>>(B.F, B.fk, N, m, B.io);
+        CX_TRY_CUDA(h, launch_pinv_solve(B.io, m, st));
+        h->launches += 2;
+      }
+      k_mix_update<<<gN, 256, 0, st>>>(B.X, B.F, B.io + m * m + m, anderson, P.mixing_param > 0 ? P.mixing_param : 0.3, B.vin, B.fk,
+                                       B.xkm1, B.fkm1, h->d_veff, N, m);
+      h->launches++;
+      CX_TRY_CUDA(h, cudaMemcpyAsync(B.vin, h->d_veff, (size_t)N * 8, cudaMemcpyDeviceToDevice, st));
+    }
+    if ((s = scf_refresh_veff(h)) != CX_OK) return s;
+    S.count_scf++;
+    out.density_updated = 1;
+  }
+  S.count++;
+  CX_TRY_CUDA(h, cudaEventRecord(S.e1, st));
+  CX_TRY_CUDA(h, cudaEventSynchronize(S.e1));
+  float ms = 0;
+  CX_TRY_CUDA(h, cudaEventElapsedTime(&ms, S.e0, S.e1));
+  if (psi_host) {
+    size_t off = 0;
+    for (int b = 0; b < h->nblk; ++b) {
+      if ((s = cx_get_psi(h, b, psi_host + 2 * off)) != CX_OK) return s;
+      off += (size_t)N * h->blocks[b].Ns;
+    }
+  }
+  if (EigVal) std::copy(S.ev.begin(), S.ev.end(), EigVal);
+  out.step_ms = ms;
+  out.Etotal = S.Etot;
+  out.lambda_f = S.lam_f;
+  out.err = S.err;
+  out.count = S.count - 1;
+  out.n_scf = S.count_scf - 1;
+  out.converged = (S.count_scf - 1 >= 1 && S.err <= P.scf_tol && S.count_scf > P.min_scf) ? 1 : 0;
+  if (info) *info = out;
+  return CX_OK;
+}
+
+extern "C" cx_status cx_scf_finish(cx_handle h, double* EigVal, double* rho_out, double* Veff_out, cx_scf_result* res) {
+  if (!h) return CX_ERR_ARG;
+  if (!h->scf) { h->err = "cx_scf_finish: call cx_scf_init first"; return CX_ERR_STATE; }
+  ScfState& S = *h->scf;
+  ScfBufs& B = S.B;
+  const int N = h->g.N, ntot = h->nstates;
+  const cudaStream_t st = h->stream;
+  const cx_scf_params& P = S.P;
+  CX_TRY_CUDA(h, cudaStreamSynchronize(st));
+  if (P.refine && S.count_scf > 1) {
     // final FP64 refinement step: Rayleigh quotients of the psi of the last step under the potential
     // they were computed for (Veff_in), then occupations, band and entropy energy again; the
     // density-dependent terms of the last step are kept (the energy is stationary in them)
     CX_TRY_CUDA(h, cudaMemcpyAsync(B.f, h->d_veff, (size_t)N * 8, cudaMemcpyDeviceToDevice, st));
     CX_TRY_CUDA(h, cudaMemcpyAsync(h->d_veff, B.vin, (size_t)N * 8, cudaMemcpyDeviceToDevice, st));
-    s = refine_eigenvalues(h, ev.data());
+    cx_status s = refine_eigenvalues(h, S.ev.data());
     CX_TRY_CUDA(h, cudaMemcpyAsync(h->d_veff, B.f, (size_t)N * 8, cudaMemcpyDeviceToDevice, st));
     if (s != CX_OK) return s;
-    CX_TRY_CUDA(h, cudaMemcpyAsync(B.ev, ev.data(), ntot * 8, cudaMemcpyHostToDevice, st));
-    k_occupations<<<1, 1024, 0, st>>>(B.ev, B.wst, ntot, P->bet, P->occfac, P->NegCharge, P->elec_T_type == 0, B.occ, B.occout);
+    CX_TRY_CUDA(h, cudaMemcpyAsync(B.ev, S.ev.data(), ntot * 8, cudaMemcpyHostToDevice, st));
+    k_occupations<<<1, 1024, 0, st>>>(B.ev, B.wst, ntot, P.bet, P.occfac, P.NegCharge, P.elec_T_type == 0, B.occ, B.occout);
     h->launches++;
     double occout[3];
     CX_TRY_CUDA(h, cudaMemcpyAsync(occout, B.occout, sizeof(occout), cudaMemcpyDeviceToHost, st));
     CX_TRY_CUDA(h, cudaStreamSynchronize(st));
-    const double Exc = sums[0] - C2 * sums[1], Exc_dc = sums[2], Eelec_dc = 0.5 * sums[3], Escc = sums[4];
-    Etot = occout[1] + Exc - Exc_dc + Eelec_dc - P->Eself + P->E_corr + occout[2] + Escc;
-    lam_f = occout[0];
+    S.Etot = total_energy(S, occout);
+    S.lam_f = occout[0];
   }
-  std::copy(ev.begin(), ev.end(), EigVal);
+  if (EigVal) std::copy(S.ev.begin(), S.ev.end(), EigVal);
   if (rho_out) CX_TRY_CUDA(h, cudaMemcpy(rho_out, B.rho, (size_t)N * 8, cudaMemcpyDeviceToHost));
   if (Veff_out) CX_TRY_CUDA(h, cudaMemcpy(Veff_out, h->d_veff, (size_t)N * 8, cudaMemcpyDeviceToHost));
-  res->Etotal = Etot;
-  res->lambda_f = lam_f;
-  res->err = err;
-  res->n_scf = count_scf - 1;
-  res->converged = err <= P->scf_tol ? 1 : 0;
+  if (res) {
+    res->Etotal = S.Etot;
+    res->lambda_f = S.lam_f;
+    res->err = S.err;
+    res->n_scf = S.count_scf - 1;
+    res->converged = S.err <= P.scf_tol ? 1 : 0;
+  }
   return CX_OK;
+}
+
+extern "C" cx_status cx_scf(cx_handle h, const cx_scf_params* P, double* EigVal, double* rho_out, double* Veff_out, double* hist,
+                            cx_scf_result* res) {
+  if (!h || !P || !EigVal || !res) return CX_ERR_ARG;
+  cx_status s = cx_scf_init(h, P);
+  if (s != CX_OK) return s;
+  ScfState& S = *h->scf;
+  // src/scf.m:111: while (err > tol && count_SCF <= MAXIT_SCF) || count_SCF <= MINIT_SCF
+  while ((S.err > P->scf_tol && S.count_scf <= P->max_scf) || S.count_scf <= P->min_scf) {
+    if ((s = cx_scf_step(h, nullptr, nullptr, nullptr)) != CX_OK) return s;
+    if (S.count > 10 * (P->max_scf + S.rhoTrigger)) break;
+  }
+  if (hist)
+    for (size_t i = 0; i < S.hist.size() && i < 2 * (size_t)P->max_scf; ++i) hist[i] = S.hist[i];
+  return cx_scf_finish(h, EigVal, rho_out, Veff_out, res);
 }

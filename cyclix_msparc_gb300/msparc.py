@@ -151,22 +151,43 @@ class CyclixGPU:
         for name, v in (("a0", a0), ("bup", bup), ("lambda_cutoff", lambda_cutoff)):
             _host_buffer(v, np.float64, len(self.blocks), name)
 
-    def eigsolve(self, count, npl, EigVal, a0, bup, lambda_cutoff, rhoTrigger=4):
-        """Device-resident eigSolver step: arrays are updated in place."""
-        self._check_step_arrays(EigVal, a0, bup, lambda_cutoff)
-        check(self.lib, self.h, self.lib.cx_eigsolver(self.h, int(count), int(npl), int(rhoTrigger), dptr(EigVal), dptr(a0),
-                                                      dptr(bup), dptr(lambda_cutoff)))
+    def _ubgv(self, ubgv):
+        """S.upper_bound_guess_vecs as the library reads it: N x nblk complex128, column-major (or None)."""
+        if ubgv is None:
+            return None
+        u = np.asarray(ubgv)
+        if u.dtype != np.complex128 or u.shape != (self.N, len(self.blocks)) or not u.flags.f_contiguous or not u.flags.writeable:
+            raise ValueError(f"ubgv: need a writable Fortran-ordered complex128 array of shape ({self.N}, {len(self.blocks)})")
+        return u
 
-    def eigsolve_host(self, count, npl, psi_packed, EigVal, a0, bup, lambda_cutoff, rhoTrigger=4):
-        _host_buffer(psi_packed, np.complex128, self.N * int(sum(self.Ns)), "psi")
+    @staticmethod
+    def _eig_params(npl, rhoTrigger, elecgs_Count, chefsibound_flag):
+        return _lib.cx_eig_params(npl=int(npl), rhoTrigger=int(rhoTrigger), elecgs_Count=int(elecgs_Count),
+                                  chefsibound_flag=int(chefsibound_flag))
+
+    def eigsolve(self, count, npl, EigVal, a0, bup, lambda_cutoff, rhoTrigger=4, elecgs_Count=1, chefsibound_flag=0,
+                 ubgv=None):
+        """Device-resident eigSolver step (src/eigSolver.m:21-125): arrays are updated in place.
+
+        ``ubgv`` (S.upper_bound_guess_vecs, N x nblk complex128, Fortran order) is read where the
+        reference restarts the upper-bound estimate from it and receives every new estimate."""
         self._check_step_arrays(EigVal, a0, bup, lambda_cutoff)
-        check(self.lib, self.h, self.lib.cx_eigsolver_host(self.h, int(count), int(npl), int(rhoTrigger),
-                                                           cptr(psi_packed),
+        u = self._ubgv(ubgv)
+        p = self._eig_params(npl, rhoTrigger, elecgs_Count, chefsibound_flag)
+        check(self.lib, self.h, self.lib.cx_eigsolver_full(self.h, C.byref(p), int(count), cptr(u) if u is not None else None,
                                                            dptr(EigVal), dptr(a0), dptr(bup), dptr(lambda_cutoff)))
 
-    def scf(self, S, scf_tol=1e-6, poisson_tol=-1.0, max_scf=100, min_scf=3, rhoTrigger=4, maxit_poisson=1000,
-            mixing_param=0.3, refine=None):
-        """Full SCF on the device-resident psi (cx_scf); returns (result, EigVal packed, rho, Veff, history)."""
+    def eigsolve_host(self, count, npl, psi_packed, EigVal, a0, bup, lambda_cutoff, rhoTrigger=4, elecgs_Count=1,
+                      chefsibound_flag=0, ubgv=None):
+        _host_buffer(psi_packed, np.complex128, self.N * int(sum(self.Ns)), "psi")
+        self._check_step_arrays(EigVal, a0, bup, lambda_cutoff)
+        u = self._ubgv(ubgv)
+        p = self._eig_params(npl, rhoTrigger, elecgs_Count, chefsibound_flag)
+        check(self.lib, self.h, self.lib.cx_eigsolver_full_host(self.h, C.byref(p), int(count),
+                                                                cptr(u) if u is not None else None, cptr(psi_packed),
+                                                                dptr(EigVal), dptr(a0), dptr(bup), dptr(lambda_cutoff)))
+
+    def _scf_params(self, S, scf_tol, poisson_tol, max_scf, min_scf, rhoTrigger, maxit_poisson, mixing_param, refine):
         xc = S.extra.get("xc", "LDA_PW") if hasattr(S, "extra") else "LDA_PW"
         if xc != "LDA_PW":
             raise CxError(_lib.CX_ERR_ARG, f"cx_scf implements LDA_PW, not {xc}")
@@ -178,6 +199,12 @@ class CyclixGPU:
                                occfac=float(S.occfac), NegCharge=float(S.NegCharge), Eself=float(S.Eself), E_corr=float(S.E_corr),
                                n_atm=int(S.n_atm), mixing_param=mixing_param, wkpt=dptr(wk), b=dptr(b), rho0=dptr(rho0),
                                refine=int(self.prec == "mixed" if refine is None else refine))
+        return p, (wk, b, rho0)
+
+    def scf(self, S, scf_tol=1e-6, poisson_tol=-1.0, max_scf=100, min_scf=3, rhoTrigger=4, maxit_poisson=1000,
+            mixing_param=0.3, refine=None):
+        """Full SCF on the device-resident psi (cx_scf); returns (result, EigVal packed, rho, Veff, history)."""
+        p, keep = self._scf_params(S, scf_tol, poisson_tol, max_scf, min_scf, rhoTrigger, maxit_poisson, mixing_param, refine)
         EV = np.zeros(int(sum(self.Ns)))
         rho = np.zeros(self.N)
         V = np.zeros(self.N)
@@ -185,6 +212,33 @@ class CyclixGPU:
         res = _lib.cx_scf_result()
         check(self.lib, self.h, self.lib.cx_scf(self.h, C.byref(p), dptr(EV), dptr(rho), dptr(V), dptr(hist), C.byref(res)))
         return res, EV, rho, V, hist[: res.n_scf]
+
+    def scf_init(self, S, scf_tol=1e-6, poisson_tol=-1.0, max_scf=100, min_scf=3, rhoTrigger=4, maxit_poisson=1000,
+                 mixing_param=0.3, refine=None):
+        """Start a caller-driven SCF (cx_scf_init): the initial potential from ``S.rho_at``."""
+        p, keep = self._scf_params(S, scf_tol, poisson_tol, max_scf, min_scf, rhoTrigger, maxit_poisson, mixing_param, refine)
+        check(self.lib, self.h, self.lib.cx_scf_init(self.h, C.byref(p)))
+
+    def scf_step(self, psi_host=None, EigVal=None):
+        """One pass of the SCF loop (cx_scf_step); ``psi_host`` (packed complex128 blocks) is copied
+        in and out around it when given.  Returns the step record (cx_scf_step_info)."""
+        info = _lib.cx_scf_step_info()
+        if psi_host is not None:
+            _host_buffer(psi_host, np.complex128, self.N * int(sum(self.Ns)), "psi")
+        if EigVal is not None:
+            _host_buffer(EigVal, np.float64, int(sum(self.Ns)), "EigVal")
+        check(self.lib, self.h, self.lib.cx_scf_step(self.h, cptr(psi_host) if psi_host is not None else None,
+                                                     dptr(EigVal) if EigVal is not None else None, C.byref(info)))
+        return info
+
+    def scf_finish(self):
+        """End the caller-driven SCF (cx_scf_finish): (result, EigVal packed, rho, Veff)."""
+        EV = np.zeros(int(sum(self.Ns)))
+        rho = np.zeros(self.N)
+        V = np.zeros(self.N)
+        res = _lib.cx_scf_result()
+        check(self.lib, self.h, self.lib.cx_scf_finish(self.h, dptr(EV), dptr(rho), dptr(V), C.byref(res)))
+        return res, EV, rho, V
 
     def poisson(self, f, phi0=None, tol=1e-8, maxit=1000):
         f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
@@ -229,6 +283,11 @@ class CyclixGPU:
     def eig_fallbacks(self) -> int:
         n = C.c_int64(0)
         check(self.lib, self.h, self.lib.cx_eig_fallback_count(self.h, C.byref(n)))
+        return n.value
+
+    def eig_hermitian(self) -> int:
+        n = C.c_int64(0)
+        check(self.lib, self.h, self.lib.cx_eig_hermitian_count(self.h, C.byref(n)))
         return n.value
 
     def launch_count(self, reset=False) -> int:
@@ -290,6 +349,10 @@ def eigSolver(S, count, upper_bound_guess_vecs, psi, EigVal, a0, bup, lambda_cut
 
     ``psi`` is N x Nev x (tnkpt*nspin) as in MATLAB (or a list of per-block N x Ns arrays for
     uneven blocks); it is copied to the GPU, updated there and copied back, like a MEX call.
+    ``S.elecgs_Count``, ``S.chefsibound_flag`` and ``S.rhoTrigger`` steer the bounds as in
+    src/eigSolver.m:21-94 (defaults 1, 0, 4).  ``upper_bound_guess_vecs`` (N x tnkpt*nspin) is
+    the start of the upper-bound estimate where the reference restarts it (later relaxation steps,
+    ``chefsibound_flag``); the returned copy holds every new estimate's vector.
     """
     gpu = S.gpu
     uniform = not isinstance(psi, (list, tuple))
@@ -300,7 +363,13 @@ def eigSolver(S, count, upper_bound_guess_vecs, psi, EigVal, a0, bup, lambda_cut
     a0 = np.ascontiguousarray(a0, dtype=np.float64).reshape(-1).copy()
     bup = np.ascontiguousarray(bup, dtype=np.float64).reshape(-1).copy()
     lc = np.ascontiguousarray(lambda_cutoff, dtype=np.float64).reshape(-1).copy()
-    gpu.eigsolve_host(count, S.npl, packed, EV, a0, bup, lc, rhoTrigger=getattr(S, "rhoTrigger", 4))
+    nblk = len(gpu.Ns)
+    if upper_bound_guess_vecs is None:
+        ubgv = np.zeros((gpu.N, nblk), dtype=np.complex128, order="F")
+    else:
+        ubgv = np.array(np.asarray(upper_bound_guess_vecs, dtype=np.complex128).reshape(gpu.N, nblk, order="F"), order="F")
+    gpu.eigsolve_host(count, S.npl, packed, EV, a0, bup, lc, rhoTrigger=getattr(S, "rhoTrigger", 4),
+                      elecgs_Count=getattr(S, "elecgs_Count", 1), chefsibound_flag=getattr(S, "chefsibound_flag", 0), ubgv=ubgv)
     out = []
     for k, n in enumerate(gpu.Ns):
         o = gpu.offsets[k] * gpu.N
@@ -311,7 +380,7 @@ def eigSolver(S, count, upper_bound_guess_vecs, psi, EigVal, a0, bup, lambda_cut
     else:
         psi_out = out
         EigVal_out = EV
-    return upper_bound_guess_vecs, psi_out, EigVal_out, a0, bup, lc
+    return ubgv, psi_out, EigVal_out, a0, bup, lc
 
 
 def scf(S, scf_tol=1e-6):

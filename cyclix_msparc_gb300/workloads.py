@@ -49,6 +49,7 @@ class Workload:
     rc: float = 1.2
     scf: bool = False
     seed: int = 0
+    zval: float = 4.0         # valence charge of each Gaussian pseudocharge (SCF workloads)
 
     @property
     def N(self) -> int:
@@ -81,6 +82,11 @@ def _make_workloads() -> dict:
     w["cyclic-batched-16nu-64x16x48-ns96to320-m24"] = Workload(
         "cyclic-batched-16nu-64x16x48-ns96to320-m24", 64, 16, 48, ns3,
         tuple((0.0, float(nu), 0.0) for nu in range(16)), 1, 24, 96, 16)
+    # the same cell, atoms and projectors as an SCF cell (Gaussian pseudocharges of valence 1, so
+    # the 48 occupied states per block fit the smallest block of 99 states)
+    w["scf-batched-16nu-64x16x48-96at-ns96to320-m24"] = Workload(
+        "scf-batched-16nu-64x16x48-96at-ns96to320-m24", 64, 16, 48, ns3,
+        tuple((0.0, float(nu), 0.0) for nu in range(16)), 1, 24, 96, 16, scf=True, zval=1.0)
     # helical twist 0.05 rad/bohr, 24 eta x 4 nu, two spin channels
     L3h = 0.2 * 40
     etas = _eta_grid(24, L3h)
@@ -276,7 +282,7 @@ def make_system(wl: Workload) -> CyclixS:
             V[:, 1] = v + _gaussian_field(S, S.Atoms, rng.uniform(-0.2, 0.2, wl.n_atm), 0.8, 6.0)
         S.Veff = V
     else:
-        Z = 4.0
+        Z = wl.zval
         sig_b = 0.6
         amp_b = -Z / (2 * np.pi * sig_b ** 2) ** 1.5
         S.b = _gaussian_field(S, S.Atoms, np.full(wl.n_atm, amp_b), sig_b, 6.0 * sig_b)

@@ -131,8 +131,9 @@ cx_status cx_hpsi(cx_handle h, int32_t blk, int32_t ncol, const double* X, doubl
 cx_status cx_chebyshev_filter(cx_handle h, int32_t blk, int32_t ncol, const double* X, double* Y,
                               int32_t m, double a, double b, double a0, int32_t prec);
 
-/* The eigSolver step over all blocks on the device-resident psi (src/eigSolver.m:26-125):
- * spectral bounds when count == 1 (Lanczos), filter cutoff, Chebyshev filter of degree npl,
+/* The eigSolver step over all blocks on the device-resident psi (src/eigSolver.m:26-125) for the
+ * first relaxation step without upper-bound vectors (cx_eigsolver_full with elecgs_Count = 1,
+ * chefsibound_flag = 0, ubgv = NULL): spectral bounds when count == 1 (Lanczos), filter cutoff, Chebyshev filter of degree npl,
  * orthonormalisation, projected Hamiltonian, general FP64 subspace eigensolver, sort,
  * rotation and W-normalisation.  EigVal is packed: block b's Ns_b values follow block b-1's.
  * a0, bup, lambda_cutoff have nblk entries each (in/out).  rhoTrigger as src/scf.m:93. */
@@ -144,9 +145,42 @@ cx_status cx_eigsolver(cx_handle h, int32_t count, int32_t npl, int32_t rhoTrigg
 cx_status cx_eigsolver_host(cx_handle h, int32_t count, int32_t npl, int32_t rhoTrigger, double* psi,
                             double* EigVal, double* a0, double* bup, double* lambda_cutoff);
 
+/* The S fields that steer eigSolver's bounds and cutoff (src/eigSolver.m:21-94). */
+typedef struct {
+  int32_t npl;               /* S.npl: Chebyshev degree */
+  int32_t rhoTrigger;        /* S.rhoTrigger (taken as 1 when elecgs_Count > 1, src/eigSolver.m:21-23) */
+  int32_t elecgs_Count;      /* S.elecgs_Count: 1 on the first relaxation / MD step, > 1 after it */
+  int32_t chefsibound_flag;  /* S.chefsibound_flag: 1 re-estimates bup from ubgv once count > rhoTrigger */
+} cx_eig_params;
+
+/* [ubgv,psi,EigVal,a0,bup,lambda_cutoff] = eigSolver(S,count,ubgv,psi,EigVal,a0,bup,lambda_cutoff)
+ * with the whole control flow of src/eigSolver.m:21-94:
+ *  - count == 1, elecgs_Count == 1: bup = 1.01 x the largest and a0 = the smallest Ritz value - 0.1
+ *    of a Lanczos run from a random vector; cutoff (bup + a0) / 2;
+ *  - count == 1, elecgs_Count > 1: bup from a Lanczos run started at ubgv, a0 = min(EigVal)
+ *    (the previous relaxation step's eigenvalues), cutoff max(EigVal) + 0.1;
+ *  - count > rhoTrigger: a0 = min(EigVal); with chefsibound_flag == 1 also bup from a Lanczos
+ *    run started at ubgv;
+ *  - otherwise the bounds are kept; cutoff max(EigVal) + 0.1.
+ * ubgv is S.upper_bound_guess_vecs: N x nblk complex (interleaved), in and out.  Every upper-bound
+ * estimate writes the Ritz vector of its largest Ritz value (2-norm 1) into the block's column;
+ * a zero column, or ubgv == NULL, starts that block from the seeded random vector (ubgv == NULL
+ * also returns no vector).  psi is device-resident (cx_set_psi / cx_get_psi). */
+cx_status cx_eigsolver_full(cx_handle h, const cx_eig_params* p, int32_t count, double* ubgv, double* EigVal, double* a0,
+                            double* bup, double* lambda_cutoff);
+/* The same with host psi in and out (blocks back to back), copied in and out by the call. */
+cx_status cx_eigsolver_full_host(cx_handle h, const cx_eig_params* p, int32_t count, double* ubgv, double* psi, double* EigVal,
+                                 double* a0, double* bup, double* lambda_cutoff);
+
 /* Number of subspace eigen-decompositions (since cx_create) that could not use the fast
  * Hermitian-plus-refinement path and ran the general FP64 solver instead. */
 cx_status cx_eig_fallback_count(cx_handle h, int64_t* count);
+/* Number of subspace eigen-decompositions (since cx_create) answered by the eigenpairs of the
+ * Hermitian part of the W-similar projected matrix: blocks of more than 512 states whose
+ * refinement did not converge, and any block whose other results would have left the rotated
+ * block ill-conditioned (eigenvalues equal to the real parts of the exact ones up to second order
+ * in the non-Hermitian part, W-orthonormal rotation). */
+cx_status cx_eig_hermitian_count(cx_handle h, int64_t* count);
 
 /* phi = aar(Lap_std, f, guess, tol, maxit, 0.6, 0.6, 7, 6, ...) (src/poissonSolve.m:36,
  * src/aar.m:1-74) with f = -4*pi*(rho+b) given; a Jacobi preconditioner replaces ILU.
@@ -203,6 +237,34 @@ typedef struct {
  * be NULL). */
 cx_status cx_scf(cx_handle h, const cx_scf_params* p, double* EigVal, double* rho, double* Veff, double* hist,
                  cx_scf_result* res);
+
+/* One SCF step at a time: the same loop as cx_scf, driven by the caller (src/scf.m:111-306).
+ * cx_scf_init sets the initial potential from p->rho0 (src/scf.m:32-39); each cx_scf_step is
+ * one pass of the loop body: the eigSolver step, occupations and, once count >= rhoTrigger, the
+ * density, Poisson solve, LDA_PW potential, energy, error and Pulay mixing; cx_scf_finish
+ * applies the optional FP64 refinement and returns the results (EigVal, rho, Veff may be NULL).
+ * The caller stops when info.converged is set or its step limit is reached, as src/scf.m:111. */
+typedef struct {
+  double Etotal;             /* free energy (Ha) after this step (of the last density update) */
+  double lambda_f;           /* Fermi level of this step's occupations */
+  double err;                /* SCF error ||Veff - Veff_in|| / ||Veff|| of the last density update */
+  int32_t count;             /* eigSolver passes so far (the reference's count) */
+  int32_t n_scf;             /* density updates so far (the reference's count_SCF - 1) */
+  int32_t density_updated;   /* 1 when this pass updated the density (count >= rhoTrigger) */
+  int32_t converged;         /* err <= scf_tol after at least min_scf density updates */
+  int32_t poisson_iters;     /* AAR iterations of this pass's Poisson solve (0 without one) */
+  int32_t pad;
+  double step_ms;            /* device time of the pass (CUDA events on the handle's stream; the
+                                copies of psi_host are outside it) */
+  double poisson_ms;         /* device time of the Poisson solve within it */
+} cx_scf_step_info;
+
+cx_status cx_scf_init(cx_handle h, const cx_scf_params* p);
+/* psi_host (may be NULL): S.psi on the host, blocks back to back (N x Ns_b complex each); copied
+ * to the device before the pass and back after it, as a MEX eigSolver call passes S.psi.
+ * EigVal (may be NULL): this pass's eigenvalues, packed over blocks. */
+cx_status cx_scf_step(cx_handle h, double* psi_host, double* EigVal, cx_scf_step_info* info);
+cx_status cx_scf_finish(cx_handle h, double* EigVal, double* rho, double* Veff, cx_scf_result* res);
 
 /* FP64 refinement of the Ritz values of the device-resident psi: lambda_j = Re(psi_j^H W H psi_j) /
  * (psi_j^H W psi_j) with H applied in complex128 (the Hamiltonian is self-adjoint in the W inner

@@ -279,6 +279,50 @@ def spectral_bounds(H, N, ks, tol=1e-2, maxit=300, complex_op=True):
     return float(np.real(lr[0])) * 1.01, float(np.real(sr[0])) - 0.1, vec[:, 0]
 
 
+def eig_solver_bounds(H, N, ks, count, ubgv, EigVal_prev, bounds, rhoTrigger=4, elecgs_Count=1, chefsibound_flag=0,
+                      tol_lanczos=1e-2, complex_op=True):
+    """Bounds and cutoff of one block, src/eigSolver.m:21-94, line by line.
+
+    ``ubgv`` is the block's column of S.upper_bound_guess_vecs, ``EigVal_prev`` its S.EigVal
+    column and ``bounds`` the previous ``(a0, bup, lambda_cutoff)``.  Returns
+    ``(a0, bup, lambda_cutoff, ubgv)``: ``ubgv`` is the eigs vector of every new upper-bound
+    estimate, else the input column.
+      * :21-23   rhoTrigger = 1 when elecgs_Count > 1;
+      * :47-64   count == 1: eigs 'lr' from rand (elecgs_Count == 1) or from ubgv (later
+                 relaxation steps), bup = 1.01 real(lambda);
+      * :65-72   count == 1: a0 = real(eigs 'sr') - 0.1, or min(EigVal) on later relaxation steps;
+      * :74-83   count > rhoTrigger: with chefsibound_flag, bup again from eigs started at ubgv;
+                 a0 = min(EigVal);
+      * :88-94   cutoff (bup + a0)/2 on the first SCF step of the first relaxation step, else
+                 max(EigVal) + 0.1.
+    """
+    a0, bup, lc = bounds
+    if elecgs_Count > 1:
+        rhoTrigger = 1
+    dt = complex if complex_op else float
+    op = spla.LinearOperator((N, N), matvec=lambda x: H(np.asarray(x, dtype=dt)), dtype=dt)
+
+    def upper(v0, tol, maxit):
+        lam, vec = spla.eigs(op, k=1, which="LR", tol=tol, maxiter=maxit, v0=np.asarray(v0, dtype=dt))
+        return float(np.real(lam[0])) * 1.01, vec[:, 0]
+
+    if count == 1:
+        if elecgs_Count == 1:
+            bup, a0, ubgv = spectral_bounds(H, N, ks, tol=tol_lanczos, maxit=300, complex_op=complex_op)
+        else:
+            bup, ubgv = upper(ubgv, tol_lanczos, 300)
+            a0 = float(np.min(EigVal_prev))
+    elif count > rhoTrigger:
+        if chefsibound_flag == 1:
+            bup, ubgv = upper(ubgv, tol_lanczos, 100)
+        a0 = float(np.min(EigVal_prev))
+    if count == 1 and elecgs_Count == 1:
+        lc = 0.5 * (bup + a0)
+    else:
+        lc = float(np.max(EigVal_prev)) + 0.10
+    return a0, bup, lc, ubgv
+
+
 def rayleigh_ritz(psi, H, S, W):
     """src/eigSolver.m:99-124: orth, Hs = psi'*H*psi, eig, real, sort, rotate, W-normalise."""
     psi = sla.orth(psi)

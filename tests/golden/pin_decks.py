@@ -13,8 +13,8 @@ Run from the repository root, where the reference tree is readable:
     python tests/golden/pin_decks.py [deck ...]        # default: LDA_CNT/C.inpt
     python tests/golden/pin_decks.py tests/Cyclix/CNT_chiral/C.inpt     # helical, Fermi-Dirac
 
-Decks are paths relative to the reference project root (``--root DIR`` reads a copy of the deck
-files elsewhere).  A deck takes ~1 min per SCF step on one core (LDA_CNT: 111,320 grid points,
+Decks are paths relative to the reference project root, taken from ``--root DIR`` or the
+CYCLIX_REFERENCE environment variable.  A deck takes ~1 min per SCF step on one core (LDA_CNT: 111,320 grid points,
 8 Bloch points, 15 states, degree 35).  ``--gpu fp64|mixed`` runs the same SCF through the GPU
 library (``CyclixGPU.scf``) instead of the oracle and records it under ``<deck>@gpu-<prec>``.
 """
@@ -30,7 +30,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path[:0] = [ROOT, os.path.join(ROOT, "tests")]
 
-REFERENCE = "/root/reference/Cyclix_MS_200220"
+# root of the reference project (the directory holding src/ and tests/)
+REFERENCE = os.environ.get("CYCLIX_REFERENCE", "")
 
 
 def out_values(out_path):
@@ -164,6 +165,8 @@ def main():
     ap.add_argument("--gpu", choices=["fp64", "mixed"], help="run the SCF through the GPU library")
     ap.add_argument("--out", default=os.path.join(HERE, "deck_pins.json"))
     args = ap.parse_args()
+    if not args.root:
+        ap.error("name the reference project root with --root or CYCLIX_REFERENCE")
     path = args.out
     for dk in args.decks:
         print(f"deck {dk}", flush=True)
