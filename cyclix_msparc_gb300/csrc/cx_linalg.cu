@@ -616,11 +616,13 @@ struct RRWork {
   int64_t* ipiv;             // LU pivots of a restart
   double2* T0;               // the W-similar matrix T, kept for the Hermitian-part eigenpairs
   double* rmin;              // smallest Cholesky diagonal of the rotation check
+  float* img;                // the rotation coefficients in the tensor-core operand layout
 };
 
 static cx_status rr_workspace(cx_handle h, int nmax, int ncolmax, RRWork& w) {
   const size_t n2 = (size_t)nmax * nmax;
-  const size_t need = n2 * 16 * 13 + nmax * 16 + nmax * 8 + 64 + n2 * 8 * 3 + (size_t)ncolmax * 8 + nmax * 4 + 64 + nmax * 8 + 64 + 44 * 256;
+  const size_t need = n2 * 16 * 13 + nmax * 16 + nmax * 8 + 64 + n2 * 8 * 3 + (size_t)ncolmax * 8 + nmax * 4 + 64 + nmax * 8 + 64 +
+                      tc_rot_image_floats(nmax, nmax) * 4 + 48 * 256;
   cx_status s = ensure(h, &h->d_rr, &h->rr_bytes, need);
   if (s != CX_OK) return s;
   char* p = (char*)h->d_rr;
@@ -649,6 +651,7 @@ static cx_status rr_workspace(cx_handle h, int nmax, int ncolmax, RRWork& w) {
   w.ipiv = (int64_t*)take((size_t)nmax * 8);
   w.T0 = (double2*)take(n2 * 16);
   w.rmin = (double*)take(64);
+  w.img = (float*)take(tc_rot_image_floats(nmax, nmax) * 4);
   return CX_OK;
 }
 
@@ -669,13 +672,10 @@ cx_status rr_gemms<double>(cx_handle h, const double2* X, const double2* HX, int
 
 template <>
 cx_status rr_gemms<float>(cx_handle h, const float2* X, const float2* HX, int N, int n, RRWork& w) {
-  const cuComplex one = make_cuComplex(1, 0), zero = make_cuComplex(0, 0);
-  CX_TRY_BLAS(h, cublasSetMathMode(h->cublas, CUBLAS_FP32_EMULATED_BF16X9_MATH));
-  CX_TRY_BLAS(h, cublasSetEmulationStrategy(h->cublas, CUBLAS_EMULATION_STRATEGY_EAGER));
-  CX_TRY_BLAS(h, cublasCgemm(h->cublas, CUBLAS_OP_C, CUBLAS_OP_N, n, n, N, &one, (const cuComplex*)X, N, (const cuComplex*)X, N,
-                             &zero, (cuComplex*)w.Gf, n));
-  CX_TRY_BLAS(h, cublasCgemm(h->cublas, CUBLAS_OP_C, CUBLAS_OP_N, n, n, N, &one, (const cuComplex*)X, N, (const cuComplex*)HX, N,
-                             &zero, (cuComplex*)w.Mf, n));
+  // Gram and projected matrices on the tensor cores (3xTF32, FP32 accumulation), then to FP64
+  cx_status s = tc_gram(h, X, X, nullptr, N, n, n, w.Gf, n);
+  if (s != CX_OK) return s;
+  if ((s = tc_gram(h, X, HX, nullptr, N, n, n, w.Mf, n)) != CX_OK) return s;
   const size_t n2 = (size_t)n * n;
   k_f2d<<<grid_for(n2), 256, 0, h->stream>>>(w.Gf, w.G, n2);
   k_f2d<<<grid_for(n2), 256, 0, h->stream>>>(w.Mf, w.Hs, n2);
@@ -683,7 +683,7 @@ cx_status rr_gemms<float>(cx_handle h, const float2* X, const float2* HX, int N,
   return CX_OK;
 }
 
-// Gw = X^H Y (complex128 result; complex64 inputs through 3xBF16 tensor-core emulation)
+// Gw = X^H Y (complex128)
 static cx_status rr_gram(cx_handle h, const double2* X, const double2* Y, int N, int n, RRWork& w) {
   const cuDoubleComplex one = make_cuDoubleComplex(1, 0), zero = make_cuDoubleComplex(0, 0);
   CX_TRY_BLAS(h, cublasSetMathMode(h->cublas, CUBLAS_DEFAULT_MATH));
@@ -691,12 +691,10 @@ static cx_status rr_gram(cx_handle h, const double2* X, const double2* Y, int N,
                              N, &zero, (cuDoubleComplex*)w.Gw, n));
   return CX_OK;
 }
-static cx_status rr_gram(cx_handle h, const float2* X, const float2* Y, int N, int n, RRWork& w) {
-  const cuComplex one = make_cuComplex(1, 0), zero = make_cuComplex(0, 0);
-  CX_TRY_BLAS(h, cublasSetMathMode(h->cublas, CUBLAS_FP32_EMULATED_BF16X9_MATH));
-  CX_TRY_BLAS(h, cublasSetEmulationStrategy(h->cublas, CUBLAS_EMULATION_STRATEGY_EAGER));
-  CX_TRY_BLAS(h, cublasCgemm(h->cublas, CUBLAS_OP_C, CUBLAS_OP_N, n, n, N, &one, (const cuComplex*)X, N, (const cuComplex*)Y, N, &zero,
-                             (cuComplex*)w.Gf, n));
+// Gw = X^H W X for complex64 X: the weights are applied on the tensor-core operand load
+static cx_status rr_wgram(cx_handle h, const float2* X, int N, int n, RRWork& w) {
+  cx_status s = tc_gram(h, X, X, h->d_W32, N, n, n, w.Gf, n);
+  if (s != CX_OK) return s;
   const size_t n2 = (size_t)n * n;
   k_f2d<<<grid_for(n2), 256, 0, h->stream>>>(w.Gf, w.Gw, n2);
   h->launches++;
@@ -717,15 +715,7 @@ cx_status rr_rotate<double>(cx_handle h, const double2* X, double2* out, int N, 
 
 template <>
 cx_status rr_rotate<float>(cx_handle h, const float2* X, float2* out, int N, int n, RRWork& w) {
-  const cuComplex one = make_cuComplex(1, 0), zero = make_cuComplex(0, 0);
-  const size_t n2 = (size_t)n * n;
-  k_d2f<<<grid_for(n2), 256, 0, h->stream>>>(w.V, w.Cf, n2);
-  h->launches++;
-  CX_TRY_BLAS(h, cublasSetMathMode(h->cublas, CUBLAS_FP32_EMULATED_BF16X9_MATH));
-  CX_TRY_BLAS(h, cublasSetEmulationStrategy(h->cublas, CUBLAS_EMULATION_STRATEGY_EAGER));
-  CX_TRY_BLAS(h, cublasCgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, N, n, n, &one, (const cuComplex*)X, N, (const cuComplex*)w.Cf, n,
-                             &zero, (cuComplex*)out, N));
-  return CX_OK;
+  return tc_rotate(h, X, w.V, N, n, n, out, w.img);
 }
 
 // Eigenpairs of the Ritz pencil A = G^-1 M (w.Hs, n x n complex128, not Hermitian for Cyclix
@@ -1029,10 +1019,15 @@ static cx_status rayleigh_ritz_block(cx_handle h, int b, int sel, RRWork& w, dou
   cplx<R>* HX = (cplx<R>*)h->bufs[2 * b + (sel ^ 1)];
   cx_status s = rr_gemms<R>(h, X, HX, N, n, w);
   if (s != CX_OK) return s;
-  // W-weighted Gram (needed by the subspace eigensolver): Gw = X^H (W X), W X in the H X buffer
-  k_wscale<R><<<col_grid(N, n), 256, 0, h->stream>>>(X, HX, (const typename WOf<R>::T*)(sizeof(R) == 4 ? (const void*)h->d_W32 : (const void*)h->d_W), N, n);
-  h->launches++;
-  if ((s = rr_gram(h, X, HX, N, n, w)) != CX_OK) return s;
+  // W-weighted Gram (needed by the subspace eigensolver): Gw = X^H (W X)
+  if constexpr (sizeof(R) == 4) {
+    if ((s = rr_wgram(h, X, N, n, w)) != CX_OK) return s;
+  } else {
+    // complex128: W X in the H X buffer, then ZGEMM
+    k_wscale<R><<<col_grid(N, n), 256, 0, h->stream>>>(X, HX, h->d_W, N, n);
+    h->launches++;
+    if ((s = rr_gram(h, X, HX, N, n, w)) != CX_OK) return s;
+  }
   // Cholesky G = R^H R (upper)
   size_t wsd = 0, wsh = 0;
   CX_TRY_SOLVER(h, cusolverDnXpotrf_bufferSize(h->cusolver, h->cusolver_params, CUBLAS_FILL_MODE_UPPER, n, CUDA_C_64F, w.G, n,
@@ -1084,6 +1079,9 @@ static cx_status rayleigh_ritz_block(cx_handle h, int b, int sel, RRWork& w, dou
   CX_TRY_CUDA(h, cudaMemcpyAsync(w.V, w.Hs, (size_t)n * n * 16, cudaMemcpyDeviceToDevice, h->stream));
   // psi = X C  (into the other buffer), then W-normalise (eigSolver.m:119-124)
   if ((s = rr_rotate<R>(h, X, HX, N, n, w)) != CX_OK) return s;
+  if constexpr (sizeof(R) == 4) {
+    if ((s = check_pipeline_status(h)) != CX_OK) return s;
+  }
   k_colnorm_w<R><<<n, 256, 0, h->stream>>>(HX, (const typename WOf<R>::T*)(sizeof(R) == 4 ? (const void*)h->d_W32 : (const void*)h->d_W), N,
                                           w.scfac);
   k_colscale<R><<<col_grid(N, n), 256, 0, h->stream>>>(HX, N, n, w.scfac);

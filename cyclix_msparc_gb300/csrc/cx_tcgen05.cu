@@ -1,0 +1,535 @@
+// Rayleigh-Ritz products of the mixed-precision path on the 5th-generation tensor cores
+// (tcgen05.mma, accumulators in tensor memory), written for sm_103a without a library:
+//
+//   gram:    C = X^H (w .* Y)      X: N x n, Y: N x m complex64 (column-major), w: optional real
+//                                  weights (N); C: n x m complex, FP32, accumulated with atomics
+//            (the Gram matrix X^H X, the projected Hamiltonian X^H (H X) and the W-Gram
+//            X^H W X of src/eigSolver.m:99-104, in the Cholesky-QR form of this library);
+//   rotate:  Z = X C               X: N x n complex64, C: n x m complex (FP64 in, split on the
+//                                  device), Z: N x m complex64 (psi * Q of src/eigSolver.m:119).
+//
+// Precision: every FP32 operand a is split into a_hi = tf32(a) (round to nearest) and
+// a_lo = a - a_hi (exact in FP32); the products a_hi b_hi + a_hi b_lo + a_lo b_hi run as three
+// kind::tf32 MMAs into one FP32 accumulator.  The dropped a_lo b_lo term and the tf32 rounding of
+// the lo parts leave a relative error near 2^-21 per product: FP32-level products ("3xTF32").
+//
+// Complex arithmetic as real GEMMs (K-major operands, K = the reduction index):
+//   gram:   with x^ = (re x_0, im x_0, re x_1, ...) and x~ = (-im x_0, re x_0, -im x_1, ...),
+//           Re C_ij = x^_i . y^_j and Im C_ij = x~_i . y^_j over K = 2N: one MMA of M = 128 rows
+//           (x^ of 64 columns of X, then x~ of the same 64) against N = 128 columns y^;
+//   rotate: Re Z = Xr Cr - Xi Ci, Im Z = Xr Ci + Xi Cr over K = n: A = the real and imaginary
+//           parts of 128 grid points of X (K-major after a register transpose), B = Cr^T, Ci^T
+//           (64 columns of C); the minus sign is the MMA's negate-B bit.
+//
+// Data movement: 4 producer warps load the operands from global memory (coalesced), split them
+// into hi / lo parts and store them in the no-swizzle K-major core-matrix layout (8 rows x 16 B
+// per core matrix, 128 B apart along K, 1 KB apart along M/N); the rotation's C image is prepared
+// once in that layout and copied per stage by cp.async.bulk.  One elected thread of a fifth warp
+// issues the MMAs; stages are handed over by mbarriers (producers -> MMA: full, MMA commit ->
+// producers: empty); the accumulator is read back with tcgen05.ld by the producer warps.
+// Every wait is bounded: on a timeout the CTA records it in *status and skips to the end, where
+// its tensor memory is released.
+#include <algorithm>
+
+#include "cx_common.h"
+
+namespace cx {
+namespace tc {
+
+constexpr int kProducerWarps = 4;
+constexpr int kThreads = 32 * (kProducerWarps + 1);
+constexpr int kTileBytes = 128 * 128;   // 128 rows x 32 tf32 (K-major core matrices)
+
+__device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(bar)) : "memory");
+}
+// expect `bytes` more transaction bytes on the current phase (no arrival)
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.expect_tx.shared::cta.b64 [%0], %1;" ::"r"(su32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(su32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait: false after about a second (2^31 SM cycles)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const long long t_end = clock64() + (1LL << 31);
+  while (clock64() < t_end)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+// generic-proxy shared-memory writes become visible to the tensor core (async proxy)
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// tensor-memory allocation (one full warp), address written to *dst
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(dst)), "r"(ncols) : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T, kind::tf32, one CTA
+__device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+// the mbarrier completes when every MMA issued so far by this thread has completed
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(bar)) : "memory");
+}
+// 16 consecutive 32-bit columns of this thread's tensor-memory lane
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]),
+        "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// shared-memory matrix descriptor: no swizzle, K-major; lbo = byte distance of core matrices
+// along K, sbo = along M/N (bits 46-47 hold the descriptor version 1)
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) | ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) |
+         ((uint64_t)1 << 46);
+}
+// instruction descriptor of kind::tf32: FP32 accumulator, A and B TF32, both K-major
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N, bool negate_b) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((negate_b ? 1u : 0u) << 14) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ float tf32_hi(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+// hi / lo parts of 4 values
+__device__ __forceinline__ void split4(float4 v, float4& hi, float4& lo) {
+  hi = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
+  lo = make_float4(v.x - hi.x, v.y - hi.y, v.z - hi.z, v.w - hi.w);
+}
+// byte offset of row r, K-chunk c (4 values) in a K-major tile of 32 K-values per row
+__device__ __forceinline__ uint32_t core_off(int r, int c) { return (uint32_t)((r >> 3) * 1024 + c * 128 + (r & 7) * 16); }
+
+// ------------------------------------------------------------------------------------ gram
+constexpr int kGramStages = 3;
+constexpr int kGramXc = 64;      // X columns per tile (MMA M = 128: x^ and x~ rows)
+constexpr int kGramN = 128;      // Y columns per tile (MMA N)
+constexpr int kGramStageBytes = 4 * kTileBytes;   // A hi, A lo, B hi, B lo
+constexpr size_t kGramSmem = 1024 + (size_t)kGramStages * kGramStageBytes;
+
+struct GramArgs {
+  const float2* X;
+  const float2* Y;
+  const float* w;           // optional weights on Y (nullptr: none)
+  float2* C;                // n x m, leading dimension ldc; accumulated (zero it first)
+  int N, n, m, ldc;
+  int kchunk;               // complex grid points per split (multiple of 16)
+  int* status;
+};
+
+__global__ void __launch_bounds__(kThreads, 1) gram_kernel(const __grid_constant__ GramArgs A) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)smem;                 // [stages]
+  uint64_t* empty = full + kGramStages;             // [stages]
+  uint64_t* done = empty + kGramStages;
+  uint32_t* tmem_slot = (uint32_t*)(done + 1);
+  int* failed = (int*)(tmem_slot + 1);
+  unsigned char* stages = smem + 1024;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i0 = blockIdx.x * kGramXc, j0 = blockIdx.y * kGramN;
+  const int kbeg = blockIdx.z * A.kchunk;
+  const int kend = min(A.N, kbeg + A.kchunk);
+  const int nk = kend > kbeg ? (kend - kbeg + 15) / 16 : 0;   // stages of 16 complex grid points
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kGramStages; ++s) {
+      mbar_init(&full[s], 32 * kProducerWarps);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(done, 1);
+    *failed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) tmem_alloc(tmem_slot, kGramN);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp < kProducerWarps) {
+    // ---- producers: 64 X columns and 128 Y columns x 16 complex grid points per stage, 16 B per piece
+    const int t = threadIdx.x;
+    for (int it = 0; it < nk && !*(volatile int*)failed; ++it) {
+      const int s = it % kGramStages;
+      if (it >= kGramStages && !mbar_wait(&empty[s], (uint32_t)(((it / kGramStages) - 1) & 1))) {
+        atomicExch(failed, 1);
+        break;
+      }
+      unsigned char* Ahi = stages + (size_t)s * kGramStageBytes;
+      unsigned char* Alo = Ahi + kTileBytes;
+      unsigned char* Bhi = Alo + kTileBytes;
+      unsigned char* Blo = Bhi + kTileBytes;
+      const int kc0 = kbeg + 16 * it;
+#pragma unroll 4
+      for (int p = t; p < (kGramXc + kGramN) * 8; p += 32 * kProducerWarps) {
+        const int col = p >> 3, q = p & 7;
+        const int k = kc0 + 2 * q;
+        const bool isx = col < kGramXc;
+        const int c = isx ? i0 + col : j0 + (col - kGramXc);
+        const float2* src = isx ? A.X : A.Y;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (c < (isx ? A.n : A.m)) {
+          const float2* colp = src + (size_t)c * A.N;
+          if (k + 1 < kend && !(A.N & 1)) {
+            v = *reinterpret_cast<const float4*>(colp + k);      // 16-byte aligned: N and k even
+          } else if (k + 1 < kend) {
+            const float2 a = colp[k], b = colp[k + 1];
+            v = make_float4(a.x, a.y, b.x, b.y);
+          } else if (k < kend) {
+            const float2 a = colp[k];
+            v = make_float4(a.x, a.y, 0.f, 0.f);
+          }
+          if (!isx && A.w) {
+            const float w0 = k < kend ? A.w[k] : 0.f, w1 = k + 1 < kend ? A.w[k + 1] : 0.f;
+            v.x *= w0; v.y *= w0; v.z *= w1; v.w *= w1;
+          }
+        }
+        float4 hi, lo;
+        if (isx) {
+          split4(v, hi, lo);
+          *reinterpret_cast<float4*>(Ahi + core_off(col, q)) = hi;
+          *reinterpret_cast<float4*>(Alo + core_off(col, q)) = lo;
+          split4(make_float4(-v.y, v.x, -v.w, v.z), hi, lo);     // x~ row
+          *reinterpret_cast<float4*>(Ahi + core_off(col + kGramXc, q)) = hi;
+          *reinterpret_cast<float4*>(Alo + core_off(col + kGramXc, q)) = lo;
+        } else {
+          split4(v, hi, lo);
+          *reinterpret_cast<float4*>(Bhi + core_off(col - kGramXc, q)) = hi;
+          *reinterpret_cast<float4*>(Blo + core_off(col - kGramXc, q)) = lo;
+        }
+      }
+      fence_async_smem();
+      mbar_arrive(&full[s]);
+    }
+  } else if (lane == 0) {
+    // ---- MMA issuer
+    constexpr uint32_t idesc = idesc_tf32(128, kGramN, false);
+    for (int it = 0; it < nk; ++it) {
+      const int s = it % kGramStages;
+      if (*(volatile int*)failed || !mbar_wait(&full[s], (uint32_t)((it / kGramStages) & 1))) {
+        atomicExch(failed, 1);
+        break;
+      }
+      tc_fence_after();
+      const uint32_t a_hi = su32(stages + (size_t)s * kGramStageBytes);
+      const uint32_t a_lo = a_hi + kTileBytes, b_hi = a_lo + kTileBytes, b_lo = b_hi + kTileBytes;
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk) {             // K = 8 per MMA: 2 core matrices of 4 values
+        const uint32_t o = kk * 256;
+        mma_tf32(tmem, smem_desc(a_hi + o, 128, 1024), smem_desc(b_hi + o, 128, 1024), idesc, (it | kk) != 0);
+        mma_tf32(tmem, smem_desc(a_hi + o, 128, 1024), smem_desc(b_lo + o, 128, 1024), idesc, 1);
+        mma_tf32(tmem, smem_desc(a_lo + o, 128, 1024), smem_desc(b_hi + o, 128, 1024), idesc, 1);
+      }
+      mma_commit(&empty[s]);
+    }
+    mma_commit(done);
+  }
+  // ---- epilogue: TMEM row m = 32 warp + lane -> Re (m < 64) or Im (m >= 64) of C[i0 + m % 64][j0 + .]
+  if (warp < kProducerWarps) {
+    bool ok = nk > 0 && !*(volatile int*)failed;
+    if (ok && !mbar_wait(done, 0)) {
+      atomicExch(failed, 1);
+      ok = false;
+    }
+    tc_fence_after();
+    const int m = 32 * warp + lane;
+    const int i = i0 + (m & 63), part = m >> 6;
+    if (__any_sync(0xffffffffu, ok)) {
+      for (int cb = 0; cb < kGramN / 16; ++cb) {
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(cb * 16), v);
+        if (ok && i < A.n) {
+#pragma unroll
+          for (int e = 0; e < 16; ++e) {
+            const int j = j0 + cb * 16 + e;
+            if (j < A.m) atomicAdd(reinterpret_cast<float*>(A.C + (size_t)j * A.ldc + i) + part, v[e]);
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x == 0 && *failed) atomicExch(A.status, 1);
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, kGramN);
+  }
+}
+
+// ------------------------------------------------------------------------------------ rotate
+constexpr int kRotStages = 2;
+constexpr int kRotM = 128;       // grid points per tile
+constexpr int kRotN = 64;        // columns of Z per tile (two accumulators: Re and Im)
+constexpr int kRotATile = kRotM * 128;   // 128 rows x 32 tf32
+constexpr int kRotBTile = kRotN * 128;   // 64 rows x 32 tf32
+constexpr int kRotStageBytes = 4 * kRotATile + 4 * kRotBTile;   // A re/im hi/lo, B cr/ci hi/lo
+constexpr size_t kRotSmem = 1024 + (size_t)kRotStages * kRotStageBytes;
+
+struct RotArgs {
+  const float2* X;          // N x n
+  const float* Cimg;        // [jt][ks] blocks of 4 B tiles (Cr hi, Cr lo, Ci hi, Ci lo) in core-matrix layout
+  float2* Z;                // N x m
+  int N, n, m;
+  int nks;                  // K stages (ceil(n / 32))
+  int* status;
+};
+
+__global__ void __launch_bounds__(kThreads, 1) rotate_kernel(const __grid_constant__ RotArgs A) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)smem;
+  uint64_t* empty = full + kRotStages;
+  uint64_t* done = empty + kRotStages;
+  uint32_t* tmem_slot = (uint32_t*)(done + 1);
+  int* failed = (int*)(tmem_slot + 1);
+  unsigned char* stages = smem + 1024;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int k0 = blockIdx.x * kRotM, jt = blockIdx.y, j0 = jt * kRotN;
+  const int nk = A.nks;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kRotStages; ++s) {
+      mbar_init(&full[s], 32 * kProducerWarps);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(done, 1);
+    *failed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) tmem_alloc(tmem_slot, 2 * kRotN);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp < kProducerWarps) {
+    for (int it = 0; it < nk && !*(volatile int*)failed; ++it) {
+      const int s = it % kRotStages;
+      if (it >= kRotStages && !mbar_wait(&empty[s], (uint32_t)(((it / kRotStages) - 1) & 1))) {
+        atomicExch(failed, 1);
+        break;
+      }
+      unsigned char* st = stages + (size_t)s * kRotStageBytes;
+      // the stage's C tiles by one bulk copy, whose bytes the phase of full[s] waits for as well
+      if (threadIdx.x == 0) {
+        const float* src = A.Cimg + ((size_t)jt * A.nks + it) * (4 * kRotBTile / 4);
+        mbar_expect_tx(&full[s], 4 * kRotBTile);
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         su32(st + 4 * kRotATile)),
+                     "l"(src), "r"((uint32_t)(4 * kRotBTile)), "r"(su32(&full[s]))
+                     : "memory");
+      }
+      // X: 128 grid points x 32 columns; a warp task = 32 points (one per lane) x 4 columns
+      const int ic0 = 32 * it;
+      for (int task = warp; task < 32; task += kProducerWarps) {
+        const int rb = task & 3, cq = task >> 2;          // row block of 32, column quad
+        const int r = 32 * rb + lane, k = k0 + r;
+        float4 re = make_float4(0.f, 0.f, 0.f, 0.f), im = re;
+        if (k < A.N) {
+          const int ib = ic0 + 4 * cq;
+          const float2* xp = A.X + (size_t)ib * A.N + k;
+          const float2 x0 = ib < A.n ? xp[0] : make_float2(0.f, 0.f);
+          const float2 x1 = ib + 1 < A.n ? xp[(size_t)A.N] : make_float2(0.f, 0.f);
+          const float2 x2 = ib + 2 < A.n ? xp[2 * (size_t)A.N] : make_float2(0.f, 0.f);
+          const float2 x3 = ib + 3 < A.n ? xp[3 * (size_t)A.N] : make_float2(0.f, 0.f);
+          re = make_float4(x0.x, x1.x, x2.x, x3.x);
+          im = make_float4(x0.y, x1.y, x2.y, x3.y);
+        }
+        float4 hi, lo;
+        split4(re, hi, lo);
+        *reinterpret_cast<float4*>(st + 0 * kRotATile + core_off(r, cq)) = hi;
+        *reinterpret_cast<float4*>(st + 1 * kRotATile + core_off(r, cq)) = lo;
+        split4(im, hi, lo);
+        *reinterpret_cast<float4*>(st + 2 * kRotATile + core_off(r, cq)) = hi;
+        *reinterpret_cast<float4*>(st + 3 * kRotATile + core_off(r, cq)) = lo;
+      }
+      fence_async_smem();
+      mbar_arrive(&full[s]);
+    }
+  } else if (lane == 0) {
+    constexpr uint32_t id_pos = idesc_tf32(kRotM, kRotN, false), id_neg = idesc_tf32(kRotM, kRotN, true);
+    const uint32_t dre = tmem, dim = tmem + kRotN;
+    for (int it = 0; it < nk; ++it) {
+      const int s = it % kRotStages;
+      if (*(volatile int*)failed || !mbar_wait(&full[s], (uint32_t)((it / kRotStages) & 1))) {
+        atomicExch(failed, 1);
+        break;
+      }
+      tc_fence_after();
+      const uint32_t base = su32(stages + (size_t)s * kRotStageBytes);
+      const uint32_t xr_hi = base, xr_lo = base + kRotATile, xi_hi = base + 2 * kRotATile, xi_lo = base + 3 * kRotATile;
+      const uint32_t cb = base + 4 * kRotATile;
+      const uint32_t cr_hi = cb, cr_lo = cb + kRotBTile, ci_hi = cb + 2 * kRotBTile, ci_lo = cb + 3 * kRotBTile;
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk) {
+        const uint32_t o = kk * 256;
+        auto d = [&](uint32_t a) { return smem_desc(a + o, 128, 1024); };
+        const uint32_t first = (it | kk) != 0;
+        // Re Z += Xr Cr - Xi Ci
+        mma_tf32(dre, d(xr_hi), d(cr_hi), id_pos, first);
+        mma_tf32(dre, d(xr_hi), d(cr_lo), id_pos, 1);
+        mma_tf32(dre, d(xr_lo), d(cr_hi), id_pos, 1);
+        mma_tf32(dre, d(xi_hi), d(ci_hi), id_neg, 1);
+        mma_tf32(dre, d(xi_hi), d(ci_lo), id_neg, 1);
+        mma_tf32(dre, d(xi_lo), d(ci_hi), id_neg, 1);
+        // Im Z += Xr Ci + Xi Cr
+        mma_tf32(dim, d(xr_hi), d(ci_hi), id_pos, first);
+        mma_tf32(dim, d(xr_hi), d(ci_lo), id_pos, 1);
+        mma_tf32(dim, d(xr_lo), d(ci_hi), id_pos, 1);
+        mma_tf32(dim, d(xi_hi), d(cr_hi), id_pos, 1);
+        mma_tf32(dim, d(xi_hi), d(cr_lo), id_pos, 1);
+        mma_tf32(dim, d(xi_lo), d(cr_hi), id_pos, 1);
+      }
+      mma_commit(&empty[s]);
+    }
+    mma_commit(done);
+  }
+  if (warp < kProducerWarps) {
+    bool ok = nk > 0 && !*(volatile int*)failed;
+    if (ok && !mbar_wait(done, 0)) {
+      atomicExch(failed, 1);
+      ok = false;
+    }
+    tc_fence_after();
+    const int k = k0 + 32 * warp + lane;
+    if (__any_sync(0xffffffffu, ok)) {
+      for (int cb = 0; cb < kRotN / 16; ++cb) {
+        float vr[16], vi[16];
+        const uint32_t ta = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(cb * 16);
+        tmem_ld16(ta, vr);
+        tmem_ld16(ta + kRotN, vi);
+        if (ok && k < A.N) {
+#pragma unroll
+          for (int e = 0; e < 16; ++e) {
+            const int j = j0 + cb * 16 + e;
+            if (j < A.m) A.Z[(size_t)j * A.N + k] = make_float2(vr[e], vi[e]);
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x == 0 && *failed) atomicExch(A.status, 1);
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 2 * kRotN);
+  }
+}
+
+// C (n x m complex128, column-major) -> per (column tile jt, K stage ks) the four B tiles Cr hi,
+// Cr lo, Ci hi, Ci lo of 64 columns x 32 rows in the K-major core-matrix layout; zero outside C.
+__global__ void k_rot_image(const double2* __restrict__ C, int n, int m, int nks, float* __restrict__ img) {
+  const int njt = (m + kRotN - 1) / kRotN;
+  const size_t per = (size_t)kRotN * 32;                   // values per tile
+  const size_t tot = (size_t)njt * nks * per;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < tot; idx += (size_t)gridDim.x * blockDim.x) {
+    const size_t blk = idx / per;
+    const int e = (int)(idx % per);
+    const int jr = e / 32, kr = e % 32;                    // row (column j of C) and K index within the tile
+    const int jt = (int)(blk / nks), ks = (int)(blk % nks);
+    const int j = jt * kRotN + jr, i = ks * 32 + kr;
+    double2 c = make_double2(0.0, 0.0);
+    if (i < n && j < m) c = C[(size_t)j * n + i];
+    const float cr = (float)c.x, ci = (float)c.y;
+    float hr, hi;
+    {
+      uint32_t r;
+      asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(cr));
+      hr = __uint_as_float(r);
+      asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(ci));
+      hi = __uint_as_float(r);
+    }
+    float* base = img + blk * 4 * per;
+    const uint32_t off = ((uint32_t)(jr >> 3) * 1024 + (uint32_t)(kr >> 2) * 128 + (uint32_t)(jr & 7) * 16) / 4 + (kr & 3);
+    base[0 * per + off] = hr;
+    base[1 * per + off] = cr - hr;
+    base[2 * per + off] = hi;
+    base[3 * per + off] = ci - hi;
+  }
+}
+
+}  // namespace tc
+
+// C (n x m, leading dimension ldc, float2) = X^H (w .* Y); C is zeroed here.
+cx_status tc_gram(cx_handle h, const float2* X, const float2* Y, const float* w, int N, int n, int m, float2* C, int ldc) {
+  using namespace tc;
+  CX_TRY_CUDA(h, cudaMemsetAsync(C, 0, (size_t)ldc * m * sizeof(float2), h->stream));
+  if (N <= 0 || n <= 0 || m <= 0) return CX_OK;
+  CX_TRY_CUDA(h, cudaFuncSetAttribute(gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGramSmem));
+  int dev = 0, nsm = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int tiles = ((n + kGramXc - 1) / kGramXc) * ((m + kGramN - 1) / kGramN);
+  // split the reduction over the grid points so that about two CTAs per SM run
+  int splits = std::max(1, (2 * nsm + tiles - 1) / tiles);
+  int kchunk = (N + splits - 1) / splits;
+  kchunk = std::max(16 * 8, (kchunk + 15) / 16 * 16);
+  splits = (N + kchunk - 1) / kchunk;
+  GramArgs a{X, Y, w, C, N, n, m, ldc, kchunk, h->d_status};
+  dim3 grid((unsigned)((n + kGramXc - 1) / kGramXc), (unsigned)((m + kGramN - 1) / kGramN), (unsigned)splits);
+  gram_kernel<<<grid, kThreads, kGramSmem, h->stream>>>(a);
+  h->launches++;
+  CX_TRY_CUDA(h, cudaGetLastError());
+  return CX_OK;
+}
+
+// Z (N x m complex64) = X (N x n complex64) C (n x m complex128); img: scratch of
+// tc_rot_image_floats(n, m) floats.
+size_t tc_rot_image_floats(int n, int m) {
+  using namespace tc;
+  const size_t njt = (m + kRotN - 1) / kRotN, nks = (n + 31) / 32;
+  return njt * nks * 4 * (size_t)kRotN * 32;
+}
+cx_status tc_rotate(cx_handle h, const float2* X, const double2* C, int N, int n, int m, float2* Z, float* img) {
+  using namespace tc;
+  if (N <= 0 || n <= 0 || m <= 0) return CX_OK;
+  CX_TRY_CUDA(h, cudaFuncSetAttribute(rotate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRotSmem));
+  const int nks = (n + 31) / 32;
+  const size_t tot = tc_rot_image_floats(n, m) / 4;
+  k_rot_image<<<(unsigned)std::min<size_t>((tot + 255) / 256, 152 * 16), 256, 0, h->stream>>>(C, n, m, nks, img);
+  RotArgs a{X, img, Z, N, n, m, nks, h->d_status};
+  dim3 grid((unsigned)((N + kRotM - 1) / kRotM), (unsigned)((m + kRotN - 1) / kRotN));
+  rotate_kernel<<<grid, kThreads, kRotSmem, h->stream>>>(a);
+  h->launches += 2;
+  CX_TRY_CUDA(h, cudaGetLastError());
+  return CX_OK;
+}
+
+}  // namespace cx

@@ -197,7 +197,9 @@ cx_status cx_poisson(cx_handle h, const double* f, double* phi, double tol, int3
  * the library (held by every GPU that loads it until exit); a call that needs more returns
  * CX_ERR_ARG naming the largest ncol that fits.  The first call on a device looks up that
  * array's address and should come before any stream capture.  Calls share the array: calls
- * whose work overlaps on the GPU race.  Each call waits for its own work before returning. */
+ * whose work overlaps on the GPU race.  Each call waits for its own work before returning.  The call
+ * runs on the handle's own stream, which is not ordered after the caller's streams: X_dev must be
+ * completely written (the caller synchronises the stream that wrote it) before the call. */
 cx_status cx_hpsi_noalloc(cx_handle h, int32_t blk, int32_t ncol, const void* X_dev, void* Y_dev, int32_t prec);
 
 /* SCF parameters: the S fields read by src/scf.m (nspin = 1, LDA_PW, potential mixing). */

@@ -78,3 +78,32 @@ def test_scf_mixed_matches_oracle(scf_system):
     for ev_ref in ref["EigVal"]:
         assert np.max(np.abs(EV[off:off + nocc] - np.array(ev_ref[:nocc]))) < 2e-5
         off += len(ev_ref)
+
+
+@pytest.mark.parametrize("case", [0, 1], ids=["cyclic", "helical"])
+def test_scf_mixed_eigenvalues_match_fp64(case):
+    """Mixed precision against plain FP64 on the GPU at a tight SCF tolerance: occupied eigenvalues
+    within 1e-6 Ha and total energy within 1e-6 Ha/atom (the target's bars), after the mixed path's
+    final FP64 refinement.  Both runs converge the potential to 1e-8 so that the comparison sees
+    the arithmetic, not the SCF tolerance."""
+    from cyclix_msparc_gb300.msparc import CyclixGPU
+    name, _, nocc = CASES[case]
+    wl = WORKLOADS[name]
+    S = make_system(wl)
+    bl = block_layout(wl, S)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        g = CyclixGPU(S, bl, prec)
+        try:
+            for i, (_, _, n) in enumerate(bl):
+                g.set_psi(i, initial_psi(S.N, n, 7 + i))
+            out[prec] = g.scf(S, scf_tol=1e-8, max_scf=80)
+        finally:
+            g.close()
+    (r64, ev64, *_), (r32, ev32, *_) = out["fp64"], out["mixed"]
+    assert r64.converged == 1 and r32.converged == 1
+    assert abs(r32.Etotal - r64.Etotal) / S.n_atm < 1e-6
+    off = 0
+    for (_, _, n) in bl:
+        assert np.max(np.abs(ev32[off:off + nocc] - ev64[off:off + nocc])) < 1e-6
+        off += n

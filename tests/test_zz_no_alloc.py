@@ -5,7 +5,8 @@ a MEX session that must leave nothing allocated) cannot let the library call cud
 entry point uses a fixed device array of the library for its projector scratch instead.  The
 test owns the device buffers (allocated through PyTorch, as such a caller would) and checks two
 calls in a row against the allocating entry point cx_hpsi, with the H*psi tolerances used by
-the other GPU tests (1e-12 relative for complex128, 2e-6 for complex64).  This file is collected
+the other GPU tests (1e-12 relative for complex128, 2e-6 for complex64), and that the second call
+leaves the device's free memory unchanged.  This file is collected
 last so that a run that stops at the first failure has already run every other test.
 """
 import ctypes as C
@@ -49,8 +50,13 @@ def test_hpsi_noalloc_matches_hpsi(small_cyclic, prec, tol):
             Xd = _to_device(torch, X, prec)
             Yd = torch.empty_like(Xd)
             torch.cuda.synchronize()
+            free0 = torch.cuda.mem_get_info()[0]
             st = g.lib.cx_hpsi_noalloc(g.h, 0, ncol, C.c_void_p(Xd.data_ptr()), C.c_void_p(Yd.data_ptr()), _lib.PREC[prec])
             assert st == _lib.CX_OK, g.lib.cx_last_error(g.h).decode()
+            torch.cuda.synchronize()
+            if call == 1:
+                # the second call (its kernels were loaded by the first) leaves the free device memory unchanged
+                assert torch.cuda.mem_get_info()[0] == free0
             got = _from_device(Yd, S.N, ncol, prec)
             err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
             assert err < tol, (call, err)
