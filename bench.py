@@ -259,6 +259,7 @@ def scf_arm(S, blocks, prec, steps, warmup, ramp, e2e_steps=0, max_passes=80, sc
         out["general_eig"] = g.eig_fallbacks() - fb0
         out["hermitian_eig"] = g.eig_hermitian() - hm0
         out["timed"] = timed
+        out["stencil_config"] = g.stencil_config()
         recs += timed
         if profile:
             g.profile(True)
@@ -317,7 +318,7 @@ def eigsolver_arm(S, blocks, prec, steps, warmup, npl, ramp=6):
             count += 1
         ms = g.timer_stop() / max(steps, 1)
         launches = g.launch_count(reset=True) / max(steps, 1)
-        paths = (g.eig_fallbacks() - fb0, g.eig_hermitian() - hm0)
+        paths = (g.eig_fallbacks() - fb0, g.eig_hermitian() - hm0, g.stencil_config())
         g.profile(True)
         g.eigsolve(count, npl, EV, a0, bup, lc)
         prof = g.profile_read() + (g.profile_read_apply(),)
@@ -499,13 +500,14 @@ def main():
     if args.only_mixed:
         S = make_system(wl)
         if not wl.scf:
-            ms, launches, (gen, herm), prof = eigsolver_arm(S, block_layout(wl, S), "mixed", args.steps, warmup, wl.npl, args.ramp)
+            ms, launches, (gen, herm, cfg), prof = eigsolver_arm(S, block_layout(wl, S), "mixed", args.steps, warmup, wl.npl,
+                                                                 args.ramp)
             n_launch, stencil_ms, stencil_bytes, apply_ms = prof
             print(json.dumps({"mode": "only-mixed", "unit": "eigSolver step", "workload": args.workload, "ms_per_step": round(ms, 3),
                               "stencil_avg_ms": round(stencil_ms / max(n_launch, 1), 4),
                               "stencil_gbs": round(stencil_bytes / (stencil_ms * 1e-3) / 1e9, 1) if stencil_ms > 0 else None,
                               "nl_apply_avg_ms": round(apply_ms / max(n_launch, 1), 4), "general_eig": gen, "hermitian_eig": herm,
-                              "launches_per_step": launches}), flush=True)
+                              "launches_per_step": launches, "stencil_config": cfg}), flush=True)
             return 0
         r = scf_arm(S, block_layout(wl, S), "mixed", args.steps, warmup, args.ramp, profile=True, max_passes=0)
         n_launch, stencil_ms, stencil_bytes, apply_ms = r["stencil"]
@@ -585,6 +587,7 @@ def main():
         "stencil_gbs": round(achieved, 1),
         "nl_apply_avg_ms": round(apply_ms / max(n_launch, 1), 4),
         "eig_paths_timed": {"general_solver": mixed["general_eig"], "hermitian_part": mixed["hermitian_eig"]},
+        "stencil_config": mixed["stencil_config"],
         "poisson": poisson_roofline(S, mixed["timed"], hbm_peak),
         "roofline": {"bound": "hbm", "kernel": "cheb_tma_kernel (fused H*psi local part + Chebyshev step, complex64)",
                      "achieved": round(achieved, 1), "peak": hbm_peak, "peak_kind": peak_kind, "unit": "GB/s",

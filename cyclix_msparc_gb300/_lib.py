@@ -22,7 +22,7 @@ EXPORTS = ["cx_create", "cx_destroy", "cx_last_error", "cx_version", "cx_set_blo
            "cx_timer_start", "cx_timer_stop", "cx_profile_stencil", "cx_profile_read", "cx_launch_count",
            "cx_host_register", "cx_host_unregister", "cx_hpsi_noalloc", "cx_profile_read_apply", "cx_eig_fallback_count", "cx_scf", "cx_refine_eigenvalues", "cx_set_device",
            "cx_eigsolver_full", "cx_eigsolver_full_host", "cx_scf_init", "cx_scf_step", "cx_scf_finish",
-           "cx_eig_hermitian_count"]
+           "cx_eig_hermitian_count", "cx_stencil_config"]
 
 
 class cx_grid(C.Structure):
@@ -117,6 +117,7 @@ def load(build_if_missing: bool = True):
         "cx_profile_read_apply": ([h, dp], C.c_int32),
         "cx_eig_fallback_count": ([h, P(C.c_int64)], C.c_int32),
         "cx_eig_hermitian_count": ([h, P(C.c_int64)], C.c_int32),
+        "cx_stencil_config": ([h, P(C.c_int32), P(C.c_int32), P(C.c_int32), C.c_char_p, C.c_int32], C.c_int32),
         "cx_scf": ([h, P(cx_scf_params), dp, dp, dp, dp, P(cx_scf_result)], C.c_int32),
         "cx_refine_eigenvalues": ([h, dp], C.c_int32),
         "cx_scf_init": ([h, P(cx_scf_params)], C.c_int32),

@@ -132,12 +132,50 @@ cx_status fused_step(cx_handle h, const BlockDev<R>* d_blocks, const StepScalars
     nlp = &nl;
   }
   const bool tma = (sizeof(R) == 4) && maps && h->use_tma;
+  if constexpr (sizeof(R) == 4) {
+    // autotuner: the first two-array step (idempotent: it does not read its output) over a full
+    // state set times every (rows per thread, prefetch depth) configuration twice and keeps the
+    // fastest for this handle; every configuration computes the same values
+    if (tma && !h->tma_tuned && !use_xprev && nstates >= 64) {
+      int rp[16], dp[16];
+      const int nc = tma_candidates(h->g, rp, dp, 16);
+      cudaEvent_t e0, e1;
+      CX_TRY_CUDA(h, cudaEventCreate(&e0));
+      CX_TRY_CUDA(h, cudaEventCreate(&e1));
+      float best = 1e30f;
+      std::string log;
+      for (int c = 0; c < nc; ++c) {
+        float tmin = 1e30f;
+        for (int rep = 0; rep < 2; ++rep) {
+          CX_TRY_CUDA(h, cudaEventRecord(e0, h->stream));
+          CX_TRY_CUDA(h, launch_cheb_step_tma(h->g, h->coef, (const BlockDev<float>*)d_blocks, d_scal, d_state_tab, nstates, in_sel,
+                                              use_xprev, *(const TmaMapSet*)maps, h->d_status, h->stream, rp[c], dp[c]));
+          CX_TRY_CUDA(h, cudaEventRecord(e1, h->stream));
+          CX_TRY_CUDA(h, cudaEventSynchronize(e1));
+          float ms = 0;
+          CX_TRY_CUDA(h, cudaEventElapsedTime(&ms, e0, e1));
+          tmin = std::min(tmin, ms);
+        }
+        h->launches += 2;
+        log += (log.empty() ? "" : " ") + std::to_string(rp[c]) + "/" + std::to_string(dp[c]) + ":" + std::to_string(tmin);
+        if (tmin < best) {
+          best = tmin;
+          h->tma_rpt = rp[c];
+          h->tma_depth = dp[c];
+        }
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      h->tma_tuned = true;
+      h->tma_tuning = log;
+    }
+  }
   if (h->prof) CX_TRY_CUDA(h, cudaEventRecord(h->ev0, h->stream));
   if constexpr (sizeof(R) == 4) {
     if (tma) {
       // stencil without the projector term, then the projector apply on the touched row chunks
       CX_TRY_CUDA(h, launch_cheb_step_tma(h->g, h->coef, (const BlockDev<float>*)d_blocks, d_scal, d_state_tab, nstates, in_sel,
-                                          use_xprev, *(const TmaMapSet*)maps, h->d_status, h->stream));
+                                          use_xprev, *(const TmaMapSet*)maps, h->d_status, h->stream, h->tma_rpt, h->tma_depth));
     }
   }
   if (!tma)
@@ -810,6 +848,19 @@ cx_status cx_host_unregister(void* ptr) {
   if (!ptr) return CX_ERR_ARG;
   cudaError_t e = cudaHostUnregister(ptr);
   if (e != cudaSuccess) { g_create_err = std::string("cx_host_unregister: ") + cudaGetErrorString(e); return CX_ERR_CUDA; }
+  return CX_OK;
+}
+
+cx_status cx_stencil_config(cx_handle h, int32_t* rows_per_thread, int32_t* ring_depth, int32_t* tuned, char* log, int32_t log_bytes) {
+  if (!h || !rows_per_thread || !ring_depth || !tuned) return CX_ERR_ARG;
+  *rows_per_thread = h->tma_rpt;
+  *ring_depth = h->tma_depth;
+  *tuned = h->tma_tuned ? 1 : 0;
+  if (log && log_bytes > 0) {
+    const size_t n = std::min((size_t)log_bytes - 1, h->tma_tuning.size());
+    std::copy(h->tma_tuning.begin(), h->tma_tuning.begin() + n, log);
+    log[n] = 0;
+  }
   return CX_OK;
 }
 

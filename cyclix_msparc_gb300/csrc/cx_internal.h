@@ -121,11 +121,25 @@ struct TmaMapSet {
 bool tma_eligible(const GridDev& g, int elem_bytes);
 cudaError_t launch_cheb_step_tma(const GridDev& g, const StencilCoef& coef, const BlockDev<float>* blocks, const StepScalars* scal,
                                  const int2* state_tab, int nstates, int in_sel, bool use_xprev, const TmaMapSet& maps, int* status,
-                                 cudaStream_t st);
+                                 cudaStream_t st, int rpt = 0, int depth = 0);
+// (rows per thread, prefetch depth) configurations of the TMA kernel for this grid (autotuner)
+int tma_candidates(const GridDev& g, int* rpt, int* depth, int cap);
 
 }  // namespace cx
 
 // ---------------------------------------------------------------- the handle
+// Resources of one concurrent Rayleigh-Ritz worker (its own stream, library handles and
+// workspaces), kept by the handle between eigSolver calls.
+struct cx_rr_worker {
+  cudaStream_t stream = nullptr;
+  cublasHandle_t cublas = nullptr;
+  cusolverDnHandle_t cusolver = nullptr;
+  cusolverDnParams_t params = nullptr;
+  void* d_ws = nullptr; size_t ws_bytes = 0;
+  void* h_ws = nullptr; size_t hws_bytes = 0;
+  void* d_rr = nullptr; size_t rr_bytes = 0;
+};
+
 struct cx_handle_s {
   std::string err;
   int dev = 0;
@@ -193,6 +207,9 @@ struct cx_handle_s {
   bool tma_ok = false;                               // operator eligible for the TMA kernel
   int* d_status = nullptr;
   bool use_tma = true;
+  int tma_rpt = 0, tma_depth = 0;                    // TMA kernel configuration (0: default rule)
+  bool tma_tuned = false;                            // the autotuner has chosen it for this handle
+  std::string tma_tuning;                            // candidates and times of the last tuning (ms)
 
   // profiling
   bool prof = false;
@@ -204,6 +221,7 @@ struct cx_handle_s {
   int64_t eig_restarts = 0;                          // similarity restarts of the eigenvector refinement
   int64_t eig_hermitian = 0;                         // subspace eigensolves answered by the Hermitian part
   int restart_fail_streak = 0;                       // blocks in a row whose restarts ended in the general solver
+  std::vector<cx_rr_worker> rr_workers;              // concurrent Rayleigh-Ritz of the blocks
 };
 
 #define CX_TRY_CUDA(h, expr)                                                                 \

@@ -16,6 +16,7 @@
 #include <cmath>
 #include <complex>
 #include <numeric>
+#include <thread>
 
 #include "cx_common.h"
 
@@ -1090,6 +1091,93 @@ static cx_status rayleigh_ritz_block(cx_handle h, int b, int sel, RRWork& w, dou
   return CX_OK;
 }
 
+// The Rayleigh-Ritz steps of all blocks.  Each block's step is a chain of small dependent
+// operations (Gram products, Cholesky, the subspace eigensolver with its convergence tests on the
+// host), so the blocks run concurrently: up to kRRWorkers host threads, each with its own stream,
+// cuBLAS / cuSOLVER handles and workspace (a copy of the handle that points at them), take the
+// blocks in turn.  The workers start after the filtered block and H X are complete on the handle's
+// stream, and the handle continues after every worker has finished.
+constexpr int kRRWorkers = 8;
+
+static cx_status make_worker(cx_handle h, cx_rr_worker& wk) {
+  CX_TRY_CUDA(h, cudaStreamCreateWithFlags(&wk.stream, cudaStreamNonBlocking));
+  if (cublasCreate(&wk.cublas) != CUBLAS_STATUS_SUCCESS || cublasSetStream(wk.cublas, wk.stream) != CUBLAS_STATUS_SUCCESS ||
+      cusolverDnCreate(&wk.cusolver) != CUSOLVER_STATUS_SUCCESS || cusolverDnSetStream(wk.cusolver, wk.stream) != CUSOLVER_STATUS_SUCCESS ||
+      cusolverDnCreateParams(&wk.params) != CUSOLVER_STATUS_SUCCESS) {
+    h->err = "eigensolver: creating the library handles of a Rayleigh-Ritz worker failed";
+    return CX_ERR_LIB;
+  }
+  return CX_OK;
+}
+
+template <typename R>
+static cx_status rayleigh_ritz_all(cx_handle h, int sel, int nmax, const std::vector<int>& off, double* EigVal) {
+  const int nblk = h->nblk;
+  const int nw = std::min(nblk, kRRWorkers);
+  cx_status s;
+  if (nw <= 1) {
+    RRWork w{};
+    if ((s = rr_workspace(h, nmax, nmax, w)) != CX_OK) return s;
+    for (int b = 0; b < nblk; ++b)
+      if ((s = rayleigh_ritz_block<R>(h, b, sel, w, EigVal + off[b])) != CX_OK) return s;
+    return CX_OK;
+  }
+  while ((int)h->rr_workers.size() < nw) {
+    h->rr_workers.emplace_back();
+    if ((s = make_worker(h, h->rr_workers.back())) != CX_OK) return s;
+  }
+  cudaEvent_t ready;
+  CX_TRY_CUDA(h, cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+  CX_TRY_CUDA(h, cudaEventRecord(ready, h->stream));
+  std::vector<cx_handle_s> shadow(nw, *h);
+  std::vector<cx_status> st(nw, CX_OK);
+  for (int i = 0; i < nw; ++i) {
+    cx_rr_worker& wk = h->rr_workers[i];
+    cx_handle_s& c = shadow[i];
+    c.stream = wk.stream;
+    c.cublas = wk.cublas;
+    c.cusolver = wk.cusolver;
+    c.cusolver_params = wk.params;
+    c.d_ws = wk.d_ws; c.ws_bytes = wk.ws_bytes;
+    c.h_ws = wk.h_ws; c.hws_bytes = wk.hws_bytes;
+    c.d_rr = wk.d_rr; c.rr_bytes = wk.rr_bytes;
+    c.launches = 0; c.eig_fallbacks = 0; c.eig_hermitian = 0; c.eig_restarts = 0;
+    c.prof = false;
+    CX_TRY_CUDA(h, cudaStreamWaitEvent(wk.stream, ready, 0));
+  }
+  std::vector<std::thread> threads;
+  for (int i = 0; i < nw; ++i)
+    threads.emplace_back([&, i]() {
+      cx_handle c = &shadow[i];
+      RRWork w{};
+      st[i] = rr_workspace(c, nmax, nmax, w);
+      for (int b = i; b < nblk && st[i] == CX_OK; b += nw) st[i] = rayleigh_ritz_block<R>(c, b, sel, w, EigVal + off[b]);
+      if (cudaStreamSynchronize(c->stream) != cudaSuccess && st[i] == CX_OK) {
+        c->err = "eigensolver: a Rayleigh-Ritz worker stream failed";
+        st[i] = CX_ERR_CUDA;
+      }
+    });
+  for (auto& t : threads) t.join();
+  cudaEventDestroy(ready);
+  s = CX_OK;
+  for (int i = 0; i < nw; ++i) {
+    cx_rr_worker& wk = h->rr_workers[i];
+    const cx_handle_s& c = shadow[i];
+    wk.d_ws = c.d_ws; wk.ws_bytes = c.ws_bytes;
+    wk.h_ws = c.h_ws; wk.hws_bytes = c.hws_bytes;
+    wk.d_rr = c.d_rr; wk.rr_bytes = c.rr_bytes;
+    h->launches += c.launches;
+    h->eig_fallbacks += c.eig_fallbacks;
+    h->eig_hermitian += c.eig_hermitian;
+    h->eig_restarts += c.eig_restarts;
+    if (st[i] != CX_OK && s == CX_OK) {
+      s = st[i];
+      h->err = c.err;
+    }
+  }
+  return s;
+}
+
 template <typename R>
 static cx_status eigsolver_T(cx_handle h, const cx_eig_params& P, int count, double* ubgv, double* EigVal, double* a0, double* bup,
                              double* lc) {
@@ -1155,11 +1243,7 @@ static cx_status eigsolver_T(cx_handle h, const cx_eig_params& P, int count, dou
   // ---- Rayleigh-Ritz per block
   int nmax = 0;
   for (int b = 0; b < nblk; ++b) nmax = std::max(nmax, h->blocks[b].Ns);
-  RRWork w{};
-  if ((s = rr_workspace(h, nmax, nmax, w)) != CX_OK) return s;
-  for (int b = 0; b < nblk; ++b) {
-    if ((s = rayleigh_ritz_block<R>(h, b, sel, w, EigVal + off[b])) != CX_OK) return s;
-  }
+  if ((s = rayleigh_ritz_all<R>(h, sel, nmax, off, EigVal)) != CX_OK) return s;
   h->psi_sel[0] = sel ^ 1;
   CX_TRY_CUDA(h, cudaStreamSynchronize(h->stream));
   return CX_OK;
@@ -1211,6 +1295,17 @@ cx_status cx_dev_to_host(cx_handle h, const void* dev, double* host, size_t n, i
 
 void cx_free_extra(cx_handle h) {
   cx::scf_state_free(h);
+  for (auto& wk : h->rr_workers) {
+    if (wk.stream) cudaStreamSynchronize(wk.stream);
+    cudaFree(wk.d_ws);
+    cudaFreeHost(wk.h_ws);
+    cudaFree(wk.d_rr);
+    if (wk.params) cusolverDnDestroyParams(wk.params);
+    if (wk.cusolver) cusolverDnDestroy(wk.cusolver);
+    if (wk.cublas) cublasDestroy(wk.cublas);
+    if (wk.stream) cudaStreamDestroy(wk.stream);
+  }
+  h->rr_workers.clear();
   cudaFree(h->d_stage); h->d_stage = nullptr;
   cudaFree(h->d_rr); h->d_rr = nullptr;
   cudaFree(h->d_lz); h->d_lz = nullptr;

@@ -44,7 +44,8 @@ constexpr int TM_TR = 32;      // radial points per tile (one per lane)
 constexpr int TM_BW = TM_TR + 2 * TM_F;   // staged row width (complex64), 352 B
 constexpr int TM_HALO = 8;     // theta halo rows staged above / below the tile (FDn used)
 constexpr int TM_PMAX = 8;     // X planes prefetched ahead of the consumer, at most
-constexpr int TM_MAXW = 12;    // warps per CTA at most (the latency of the plane pipeline wants the most warps)
+constexpr int TM_MAXW = 12;    // warps per CTA at most with 2 or 3 rows per thread (register budget of 12 warps)
+constexpr int TM_MAXW1 = 16;   // warps per CTA at most with one row per thread
 constexpr size_t TM_SMEM_MAX = 200 * 1024;
 
 struct TmaArgs {
@@ -135,7 +136,7 @@ __device__ __forceinline__ float2 forward_row(float2 (&acc)[TM_Q], float2 x, flo
 
 // RPT: theta rows per thread, HEL: helical cross term
 template <int RPT, bool HEL>
-__global__ void __launch_bounds__(TM_MAXW * 32, 1) cheb_tma_kernel(const __grid_constant__ TmaArgs A) {
+__global__ void __launch_bounds__((RPT == 1 ? TM_MAXW1 : TM_MAXW) * 32, 1) cheb_tma_kernel(const __grid_constant__ TmaArgs A) {
   constexpr int F = TM_F, Q = TM_Q, BW = TM_BW, H = TM_HALO;
   extern __shared__ __align__(128) unsigned char smem[];
   const int Nx = A.g.Nx, Ny = A.g.Ny, Nz = A.g.Nz;
@@ -434,7 +435,9 @@ static size_t tma_smem_bytes(const TileGeom& t) {
 // Theta tiling: one tile of all Ny rows when Ny <= 24 (helical cells: <= 36), else the fewest
 // equal tiles of <= 24 rows.  Tile rows must be a multiple of 4 so that every staged row block
 // starts on a 128-byte boundary (row pitch 352 B), and >= the 8-row halo.
-static bool tile_geometry(const GridDev& g, TileGeom* t) {
+// rpt (rows per thread) and prefetch depth: the given ones when valid (rpt > 0, p > 0), else
+// the default rule: the fewest rows per thread with at most 12 warps, the deepest prefetch that fits.
+static bool tile_geometry(const GridDev& g, TileGeom* t, int rpt = 0, int p_req = 0) {
   // (z wraps at most once: Nz >= FDn)
   if (g.FDn != TM_F || g.BCy != 0 || g.Ny < TM_HALO || g.Nz < TM_F) return false;
   int ty = 0, nt = 0;
@@ -447,18 +450,31 @@ static bool tile_geometry(const GridDev& g, TileGeom* t) {
   if (ty == 0) return false;
   t->TY = ty;
   t->tiles_t = nt;
-  t->rpt = (ty + TM_MAXW - 1) / TM_MAXW;
-  if (t->rpt > 3) return false;
+  t->rpt = rpt > 0 ? rpt : (ty + TM_MAXW - 1) / TM_MAXW;
+  if (t->rpt < 1 || t->rpt > 3) return false;
   t->warps = (ty + t->rpt - 1) / t->rpt;
+  if (t->warps > (t->rpt == 1 ? TM_MAXW1 : TM_MAXW)) return false;
   t->stage_bytes = TM_BW * (ty + 2 * TM_HALO) * 8 + 32 * ty * 4;   // rows + Veff tile
   t->ostage_bytes = 32 * ty * 8;                                    // previous iterate tile
-  // the deepest prefetch (P X planes and P xprev tiles in flight) that fits
-  for (int p = TM_PMAX; p >= 2; --p) {
+  // the deepest prefetch (P X planes and P xprev tiles in flight) that fits, or the requested one
+  for (int p = p_req > 0 ? p_req : TM_PMAX; p >= 2; --p) {
     t->nst = 1 + p;
     t->nos = p;
     if (tma_smem_bytes(*t) <= TM_SMEM_MAX) return true;
+    if (p_req > 0) return false;
   }
   return false;
+}
+
+// (rows per thread, prefetch depth) candidates of the autotuner for this grid
+int tma_candidates(const GridDev& g, int* rpt, int* depth, int cap) {
+  int n = 0;
+  for (int r = 1; r <= 3; ++r)
+    for (int p = 2; p <= TM_PMAX; p += 2) {
+      TileGeom t;
+      if (n < cap && tile_geometry(g, &t, r, p)) { rpt[n] = r; depth[n] = p; ++n; }
+    }
+  return n;
 }
 
 bool tma_eligible(const GridDev& g, int elem_bytes) {
@@ -522,9 +538,9 @@ static cudaError_t launch_tma_inst(const TmaArgs& a, dim3 grid, int threads, siz
 
 cudaError_t launch_cheb_step_tma(const GridDev& g, const StencilCoef& coef, const BlockDev<float>* blocks, const StepScalars* scal,
                                  const int2* state_tab, int nstates, int in_sel, bool use_xprev, const TmaMapSet& maps, int* status,
-                                 cudaStream_t st) {
+                                 cudaStream_t st, int rpt, int depth) {
   TileGeom t;
-  if (!tile_geometry(g, &t)) return cudaErrorInvalidValue;
+  if (!tile_geometry(g, &t, rpt, depth)) return cudaErrorInvalidValue;
   TmaArgs a{};
   a.g = g;
   a.blocks = blocks;

@@ -8,10 +8,11 @@
 //   rotate:  Z = X C               X: N x n complex64, C: n x m complex (FP64 in, split on the
 //                                  device), Z: N x m complex64 (psi * Q of src/eigSolver.m:119).
 //
-// Precision: every FP32 operand a is split into a_hi = tf32(a) (round to nearest) and
-// a_lo = a - a_hi (exact in FP32); the products a_hi b_hi + a_hi b_lo + a_lo b_hi run as three
-// kind::tf32 MMAs into one FP32 accumulator.  The dropped a_lo b_lo term and the tf32 rounding of
-// the lo parts leave a relative error near 2^-21 per product: FP32-level products ("3xTF32").
+// Precision: every FP32 operand a is split into a_hi = tf32(a) and a_lo = tf32(a - a_hi) (both
+// rounded to nearest, so a_hi + a_lo represents a to 2^-22 relative); the products
+// a_hi b_hi + a_hi b_lo + a_lo b_hi run as three kind::tf32 MMAs into one FP32 accumulator.  The
+// dropped a_lo b_lo term and the representation leave a relative error of a few 2^-22 per
+// product, unbiased: FP32-level products ("3xTF32").
 //
 // Complex arithmetic as real GEMMs (K-major operands, K = the reduction index):
 //   gram:   with x^ = (re x_0, im x_0, re x_1, ...) and x~ = (-im x_0, re x_0, -im x_1, ...),
@@ -124,10 +125,11 @@ __device__ __forceinline__ float tf32_hi(float x) {
   asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
   return __uint_as_float(r);
 }
-// hi / lo parts of 4 values
+// hi / lo parts of 4 values, both rounded to tf32 here (the MMA would otherwise truncate the
+// low 13 bits of lo, a biased error of up to 2^-21 |a| instead of an unbiased 2^-22 |a|)
 __device__ __forceinline__ void split4(float4 v, float4& hi, float4& lo) {
   hi = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
-  lo = make_float4(v.x - hi.x, v.y - hi.y, v.z - hi.z, v.w - hi.w);
+  lo = make_float4(tf32_hi(v.x - hi.x), tf32_hi(v.y - hi.y), tf32_hi(v.z - hi.z), tf32_hi(v.w - hi.w));
 }
 // byte offset of row r, K-chunk c (4 values) in a K-major tile of 32 K-values per row
 __device__ __forceinline__ uint32_t core_off(int r, int c) { return (uint32_t)((r >> 3) * 1024 + c * 128 + (r & 7) * 16); }
@@ -479,9 +481,9 @@ __global__ void k_rot_image(const double2* __restrict__ C, int n, int m, int nks
     float* base = img + blk * 4 * per;
     const uint32_t off = ((uint32_t)(jr >> 3) * 1024 + (uint32_t)(kr >> 2) * 128 + (uint32_t)(jr & 7) * 16) / 4 + (kr & 3);
     base[0 * per + off] = hr;
-    base[1 * per + off] = cr - hr;
+    base[1 * per + off] = tf32_hi(cr - hr);
     base[2 * per + off] = hi;
-    base[3 * per + off] = ci - hi;
+    base[3 * per + off] = tf32_hi(ci - hi);
   }
 }
 

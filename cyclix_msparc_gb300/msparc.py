@@ -290,6 +290,13 @@ class CyclixGPU:
         check(self.lib, self.h, self.lib.cx_eig_hermitian_count(self.h, C.byref(n)))
         return n.value
 
+    def stencil_config(self) -> dict:
+        """The complex64 stencil kernel's configuration and the autotuner's log (cx_stencil_config)."""
+        r, d, t = C.c_int32(0), C.c_int32(0), C.c_int32(0)
+        buf = C.create_string_buffer(1024)
+        check(self.lib, self.h, self.lib.cx_stencil_config(self.h, C.byref(r), C.byref(d), C.byref(t), buf, 1024))
+        return {"rows_per_thread": r.value, "ring_depth": d.value, "tuned": bool(t.value), "candidates_ms": buf.value.decode()}
+
     def launch_count(self, reset=False) -> int:
         n = C.c_int64(0)
         check(self.lib, self.h, self.lib.cx_launch_count(self.h, C.byref(n), 1 if reset else 0))

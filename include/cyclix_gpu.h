@@ -289,6 +289,10 @@ cx_status cx_profile_read_apply(cx_handle h, double* apply_ms);
 /* Page-lock a caller-owned host buffer for faster copies (cudaHostRegister) and release it. */
 cx_status cx_host_register(void* ptr, size_t bytes);
 cx_status cx_host_unregister(void* ptr);
+/* Configuration of the complex64 stencil kernel on h: rows per thread and TMA prefetch depth
+ * (0: the default rule), whether the autotuner chose them (it times every configuration on the
+ * first full-size filter step of the handle), and its log ("rows/depth:ms ...", may be NULL). */
+cx_status cx_stencil_config(cx_handle h, int32_t* rows_per_thread, int32_t* ring_depth, int32_t* tuned, char* log, int32_t log_bytes);
 /* Number of this library's kernel launches issued on h since the last reset. */
 cx_status cx_launch_count(cx_handle h, int64_t* count, int32_t reset);
 

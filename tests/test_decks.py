@@ -213,3 +213,20 @@ def test_force_pin_record(deck, tol):
     Fr = np.array(rec["reference"]["forces"])
     assert F.shape == Fr.shape
     assert np.max(np.abs(F - Fr)) <= tol, np.max(np.abs(F - Fr))
+
+
+def test_deck_fixtures_rebuild_the_setup():
+    """tests/golden/deck_<name>.npz rebuilds a consistent CyclixS: the atomic density guess holds
+    the valence charge, and (where the reference tree is set) the fixture equals a fresh set-up."""
+    from golden.make_deck_fixtures import DECKS, load
+    for name, rel in DECKS.items():
+        S, scf_tol, poisson_tol, e_ref = load(name)
+        assert S.W.shape == (S.N,) and S.b.shape == (S.N,)
+        assert abs(float(S.W @ S.rho_at) + S.NegCharge) < 1e-6 * abs(S.NegCharge)
+        assert e_ref < 0 and 0 < scf_tol <= 1e-4
+        if REF and os.path.exists(os.path.join(REF, rel)):
+            from cyclix_msparc_gb300.deck import load_deck
+            d = load_deck(os.path.join(REF, rel), overrides=_ran_with(rel))
+            assert np.array_equal(d.S.b, S.b) and np.array_equal(d.S.rho_at, S.rho_at)
+            assert sum(img.rc_pos.size for A in d.S.Atom for img in A.rcImage) == sum(
+                img.rc_pos.size for A in S.Atom for img in A.rcImage)

@@ -1,0 +1,38 @@
+"""The GPU SCF on two of the reference's own Cyclix decks against the free energy the reference
+printed for them (tests/Cyclix/CNT_chiral/C.out: helical, twist 0.1636 rad/bohr, Gamma point;
+tests/Cyclix/CNT_ABINITmatch/C.out: cyclic, 9 Bloch points; both LDA_PW with Fermi-Dirac
+smearing and psp8 projectors of two projectors per l <= 1, passed to the library as 4-column
+atoms).  The deck set-up comes from tests/golden/deck_<name>.npz (written by
+tests/golden/make_deck_fixtures.py from the reference's deck files with this library's psp8
+loader), so the test needs no reference tree.
+
+Tolerance: free energy per atom within 1e-6 Ha/atom of the printed value (the oracle SCF from the
+same set-up is within 9.0e-8 and 2.7e-9 of it), in FP64 and in mixed precision.
+"""
+import numpy as np
+import pytest
+
+from golden.make_deck_fixtures import load
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", ["CNT_chiral", "CNT_ABINITmatch"])
+def test_deck_free_energy_matches_printed(name, prec):
+    from cyclix_msparc_gb300.msparc import CyclixGPU
+    from cyclix_msparc_gb300.workloads import initial_psi
+    S, scf_tol, poisson_tol, e_ref = load(name)
+    blocks = [(S.kptgrid[k].copy(), 0, S.Nev) for k in range(S.tnkpt)]
+    g = CyclixGPU(S, blocks, prec)
+    try:
+        for b in range(len(blocks)):
+            g.set_psi(b, initial_psi(S.N, S.Nev, 700 + b))
+        res, EV, rho, V, hist = g.scf(S, scf_tol=min(scf_tol, 1e-6), poisson_tol=poisson_tol, max_scf=60)
+    finally:
+        g.close()
+    assert res.converged == 1
+    e = res.Etotal / S.n_atm
+    assert abs(e - e_ref) < 1e-6, (name, prec, e, e_ref)
+    # the electron count is conserved
+    assert abs(float(np.sum(rho * S.W)) + S.NegCharge) < 1e-8 * abs(S.NegCharge)
