@@ -1253,7 +1253,29 @@ static cx_status eigsolver_T(cx_handle h, const cx_eig_params& P, int count, dou
 
 using namespace cx;
 
+// Device alias of page-locked host memory (registered or allocated page-locked), or null for
+// pageable memory.  On Grace-Blackwell the GPU reads and writes such memory over NVLink-C2C, so the
+// complex64 path converts straight between the caller's complex128 host array and the device
+// buffer in one kernel, without a staging copy.
+static void* mapped_alias(const void* host) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+    cudaGetLastError();                       // (pageable memory on older drivers reports an error)
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 cx_status cx_host_to_dev(cx_handle h, const double* host, void* dev, size_t n, int prec) {
+  if (prec != CX_PREC_FP64) {
+    if (const void* alias = mapped_alias(host)) {
+      k_d2f<<<grid_for(n), 256, 0, h->stream>>>((const double2*)alias, (float2*)dev, n);
+      h->launches++;
+      CX_TRY_CUDA(h, cudaGetLastError());
+      CX_TRY_CUDA(h, cudaStreamSynchronize(h->stream));
+      return CX_OK;
+    }
+  }
   if (prec == CX_PREC_FP64) {
     CX_TRY_CUDA(h, cudaMemcpyAsync(dev, host, n * 16, cudaMemcpyHostToDevice, h->stream));
     CX_TRY_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -1274,6 +1296,15 @@ cx_status cx_host_to_dev(cx_handle h, const double* host, void* dev, size_t n, i
 }
 
 cx_status cx_dev_to_host(cx_handle h, const void* dev, double* host, size_t n, int prec) {
+  if (prec != CX_PREC_FP64) {
+    if (void* alias = mapped_alias(host)) {
+      k_f2d<<<grid_for(n), 256, 0, h->stream>>>((const float2*)dev, (double2*)alias, n);
+      h->launches++;
+      CX_TRY_CUDA(h, cudaGetLastError());
+      CX_TRY_CUDA(h, cudaStreamSynchronize(h->stream));
+      return CX_OK;
+    }
+  }
   if (prec == CX_PREC_FP64) {
     CX_TRY_CUDA(h, cudaMemcpyAsync(host, dev, n * 16, cudaMemcpyDeviceToHost, h->stream));
     CX_TRY_CUDA(h, cudaStreamSynchronize(h->stream));

@@ -88,46 +88,48 @@ __global__ void k_pois_pinv(double* __restrict__ io, int m) {
 // ---------------------------------------------------------------------------- persistent AAR
 struct AarArgs {
   int Nx, Ny, Nz, N, F, helical, bcy, bcz;
-  double xin, dx, twist;
   double cr2[kMaxFDn + 1], cr1[kMaxFDn + 1], ct2[kMaxFDn + 1], ct1[kMaxFDn + 1], cz2[kMaxFDn + 1], cz1[kMaxFDn + 1];
   const double* f;
   const double* dinv;
-  double* x;          // iterate
-  double* vt;         // helical: D_theta x
-  double* res;        // preconditioned residual
+  const double* rinv;     // 1 / r per radial node (Nx)
+  const double* thsc;     // theta scale per radial node: 1 / r^2, helical tau^2 + 1 / r^2 (Nx)
+  double* x0;             // iterate, two buffers (the next iterate is written while the current is read)
+  double* x1;
+  double* vt;             // helical: D_theta x
+  double* res;            // preconditioned residual
   double* xold;
   double* fold;
-  double* DX;         // N x m
-  double* DF;         // N x m
-  double* red;        // [0,1] ||r||^2 (by iteration parity), [2 .. 2+m*m+2m) normal matrix, DF'res, gamma
-  unsigned* bar;      // [0] arrivals, [1] generation
-  int* status;        // 1 when a barrier wait ran out
-  double* phi;        // result
+  double* DX;             // N x m
+  double* DF;             // N x m
+  double* part;           // per-block partial sums: [2][nblocks] ||r||^2 by iteration parity, then [nblocks][m (m + 1)]
+  double* gam;            // Anderson weights (m)
+  unsigned* bar;          // barrier arrival word
+  int* status;            // 1 when a barrier wait ran out
+  double* phi;            // result
   int* out_iters;
   double* out_relres;
   double tol, nb, omega, beta;
   int maxit, p;
 };
 
-// Grid barrier of a cooperative launch (every block resident): arrival counter and generation
-// word in global memory; the wait is bounded (about a second), after which *status is set and
-// false is returned to every thread of the block.
-__device__ __forceinline__ bool grid_barrier(unsigned* bar, int* status) {
+// Grid barrier of a cooperative launch (every block resident), in the sign-bit form: block 0 adds
+// 2^31 - (nblocks - 1) and every other block 1 to one arrival word, so its top bit flips exactly
+// when the last block arrives and the word needs no reset.  The wait is bounded (about a second),
+// after which *status is set and false is returned to every thread of the block.
+__device__ __forceinline__ bool grid_sync(unsigned* bar, int* status) {
   __shared__ int ok_s;
   __syncthreads();
   if (threadIdx.x == 0) {
-    int ok = 1;
-    volatile unsigned* gen = bar + 1;
-    const unsigned g = *gen;
+    const unsigned inc = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1) : 1u;
     __threadfence();
-    if (atomicAdd(bar, 1u) == gridDim.x - 1) {
-      atomicExch(bar, 0u);
-      __threadfence();
-      atomicAdd(bar + 1, 1u);
-    } else {
+    const unsigned old = atomicAdd(bar, inc);
+    volatile unsigned* w = bar;
+    int ok = 1;
+    if (((old ^ *w) & 0x80000000u) == 0) {
       const long long t_end = clock64() + (1LL << 31);
-      while (*gen == g) {
+      while (((old ^ *w) & 0x80000000u) == 0) {
         if (clock64() > t_end) { ok = 0; atomicExch(status, 1); break; }
+        __nanosleep(20);
       }
     }
     __threadfence();
@@ -146,6 +148,20 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
   if (threadIdx.x == 0)
     for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sh[k];
   return t;   // valid in thread 0
+}
+// sum of the n per-block partials at a (written by other blocks): every thread gets it
+__device__ __forceinline__ double sum_partials(const double* a, int n, double* sh) {
+  __shared__ double tot;
+  if (threadIdx.x < 32) {
+    double v = 0;
+    for (int i = threadIdx.x; i < n; i += 32) v += __ldcg(a + i);
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) tot = v;
+  }
+  __syncthreads();
+  const double t = tot;
+  __syncthreads();
+  return t;
 }
 
 // neighbour in theta / z with the grid's boundary conditions (k = 0: no phase); -1 when zero
@@ -170,15 +186,14 @@ __device__ double d_theta(const AarArgs& A, const double (*C)[kMaxFDn + 1], cons
 }
 
 // Lap_std x at point p (matrix-free, the arithmetic of the Hamiltonian kernels' Laplacian)
-// (coefficients C: cr2, cr1, ct2, ct1, cz2, cz1 rows, staged in shared memory)
-__device__ double lap_at(const AarArgs& A, const double (*C)[kMaxFDn + 1], const double* x, const double* vt, int p) {
+// (coefficients C: cr2, cr1, ct2, ct1, cz2, cz1 rows, staged in shared memory with 1/r and the theta scale)
+__device__ double lap_at(const AarArgs& A, const double (*C)[kMaxFDn + 1], const double* rinv, const double* thsc, const double* x,
+                         const double* vt, int p) {
   const int Nx = A.Nx, Ny = A.Ny, plane = Nx * Ny;
   const int r = p % Nx, t = (p / Nx) % Ny, z = p / plane;
   const double xc = ldx(x, p);
-  const double rr = A.xin + (double)r * A.dx;
-  const double inv_r = 1.0 / rr;
-  const double th_scale = A.helical ? A.twist * A.twist + 1.0 / (rr * rr) : 1.0 / (rr * rr);
   double s2 = C[0][0] * xc, s1 = 0, st2 = C[2][0] * xc, sz = C[4][0] * xc, sx = 0;
+#pragma unroll 2
   for (int q = 1; q <= A.F; ++q) {
     const double a = r + q < Nx ? ldx(x, p + q) : 0.0, b = r - q >= 0 ? ldx(x, p - q) : 0.0;
     s2 += C[0][q] * (a + b);
@@ -194,39 +209,53 @@ __device__ double lap_at(const AarArgs& A, const double (*C)[kMaxFDn + 1], const
       sx += C[5][q] * (u - w);
     }
   }
-  return s2 + inv_r * s1 + th_scale * st2 + sz + sx;
+  return s2 + rinv[r] * s1 + thsc[r] * st2 + sz + sx;
 }
 
+// The AAR loop of src/aar.m:55-80.  Each iteration evaluates the residual at the current iterate
+// and, on a Richardson iteration, writes the next iterate x + omega res into the other buffer in
+// the same pass; one grid barrier then publishes both and the norm.  An Anderson iteration (every
+// p-th) reduces the normal equations, solves them in block 0 and updates after two more barriers.
 __global__ void __launch_bounds__(256, 2) k_aar(const __grid_constant__ AarArgs A) {
+  extern __shared__ double rtab[];                  // 1/r and theta scale per radial node (2 Nx)
   __shared__ double sh[32];
   __shared__ double gsh[kAarM * kAarM + 2 * kAarM];
   __shared__ double C[6][kMaxFDn + 1];
+  __shared__ double relres_s;
   if (threadIdx.x <= kMaxFDn) {
     const int q = threadIdx.x;
     C[0][q] = A.cr2[q]; C[1][q] = A.cr1[q]; C[2][q] = A.ct2[q]; C[3][q] = A.ct1[q]; C[4][q] = A.cz2[q]; C[5][q] = A.cz1[q];
   }
+  for (int i = threadIdx.x; i < A.Nx; i += blockDim.x) {
+    rtab[i] = A.rinv[i];
+    rtab[A.Nx + i] = A.thsc[i];
+  }
   __syncthreads();
-  const int m = kAarM, N = A.N;
+  const double* rinv = rtab;
+  const double* thsc = rtab + A.Nx;
+  const int m = kAarM, N = A.N, nblk = gridDim.x;
   const int stride = gridDim.x * blockDim.x;
   const int tid0 = blockIdx.x * blockDim.x + threadIdx.x;
   double relres = 1 + A.tol;
   int count = 1;
-  bool alive = true;
-  while (alive && count <= A.maxit && relres > A.tol) {
+  double* xc = A.x0;
+  double* xn = A.x1;
+  while (count <= A.maxit && relres > A.tol) {
     if (A.helical) {
       for (int p = tid0; p < N; p += stride) {
         const int r = p % A.Nx, t = (p / A.Nx) % A.Ny, z = p / (A.Nx * A.Ny);
-        A.vt[p] = d_theta(A, C, A.x, r, t, z);
+        A.vt[p] = d_theta(A, C, xc, r, t, z);
       }
-      if (!grid_barrier(A.bar, A.status)) { alive = false; break; }
+      if (!grid_sync(A.bar, A.status)) break;
     }
-    // r = f - Lap x; res = dinv r; history columns; ||r||^2
+    // r = f - Lap x; res = dinv r; history columns; ||r||^2; Richardson step into the other buffer
     const int col = (count - 2 + m) % m;
+    const bool anderson = count % A.p == 0;
     double s = 0;
     for (int p = tid0; p < N; p += stride) {
-      const double rv = A.f[p] - lap_at(A, C, A.x, A.vt, p);
+      const double rv = A.f[p] - lap_at(A, C, rinv, thsc, xc, A.vt, p);
       const double pv = A.dinv[p] * rv;
-      const double xv = A.x[p];
+      const double xv = xc[p];
       s += rv * rv;
       if (count > 1) {
         A.DX[(size_t)col * N + p] = xv - A.xold[p];
@@ -235,18 +264,13 @@ __global__ void __launch_bounds__(256, 2) k_aar(const __grid_constant__ AarArgs 
       A.xold[p] = xv;
       A.fold[p] = pv;
       A.res[p] = pv;
+      if (!anderson) xn[p] = xv + A.omega * pv;
     }
     s = block_sum(s, sh);
-    if (threadIdx.x == 0) atomicAdd(A.red + (count & 1), s);
-    if (!grid_barrier(A.bar, A.status)) { alive = false; break; }
-    relres = sqrt(__ldcg(A.red + (count & 1))) * A.nb;
-    if (blockIdx.x == 0 && threadIdx.x == 0) A.red[(count + 1) & 1] = 0.0;    // next iteration's accumulator
-    if (!(relres > A.tol)) break;   // x (= xold) is the converged iterate (aar.m:57-80)
-    if (count % A.p != 0) {
-      for (int p = tid0; p < N; p += stride) A.x[p] += A.omega * A.res[p];
-    } else {
-      // normal matrix DF'DF and DF'res (block partial sums, one row of it at a time), pinv by one
-      // thread of block 0 (gamma published in red), then the update
+    if (threadIdx.x == 0) A.part[(count & 1) * nblk + blockIdx.x] = s;
+    if (anderson) {
+      // this block's share of the normal matrix DF'DF and DF'res (its own points, written above)
+      double* pa = A.part + 2 * nblk + (size_t)blockIdx.x * m * (m + 1);
       for (int i = 0; i < m; ++i) {
         double acc[kAarM + 1];
         for (int j = 0; j <= m; ++j) acc[j] = 0;
@@ -257,28 +281,39 @@ __global__ void __launch_bounds__(256, 2) k_aar(const __grid_constant__ AarArgs 
         }
         for (int j = 0; j <= m; ++j) {
           const double t = block_sum(acc[j], sh);
-          if (threadIdx.x == 0) atomicAdd(A.red + 2 + (j < m ? i * m + j : m * m + i), t);
+          if (threadIdx.x == 0) pa[j < m ? i * m + j : m * m + i] = t;
         }
-      }
-      if (!grid_barrier(A.bar, A.status)) { alive = false; break; }
-      if (blockIdx.x == 0 && threadIdx.x == 0) {
-        for (int k = 0; k < m * m + m; ++k) {
-          gsh[k] = __ldcg(A.red + 2 + k);
-          A.red[2 + k] = 0.0;                       // cleared for the next Anderson step
-        }
-        pinv_solve_1t(gsh, m);                      // gamma -> gsh[m*m + m ..]
-        for (int i = 0; i < m; ++i) A.red[2 + m * m + m + i] = gsh[m * m + m + i];
-      }
-      if (!grid_barrier(A.bar, A.status)) { alive = false; break; }
-      double gam[kAarM];
-      for (int i = 0; i < m; ++i) gam[i] = __ldcg(A.red + 2 + m * m + m + i);
-      for (int p = tid0; p < N; p += stride) {
-        double u = A.x[p] + A.beta * A.res[p];
-        for (int i = 0; i < m; ++i) u -= (A.DX[(size_t)i * N + p] + A.beta * A.DF[(size_t)i * N + p]) * gam[i];
-        A.x[p] = u;
       }
     }
-    if (!grid_barrier(A.bar, A.status)) { alive = false; break; }
+    if (!grid_sync(A.bar, A.status)) break;
+    relres = sqrt(sum_partials(A.part + (count & 1) * nblk, nblk, sh)) * A.nb;
+    if (!(relres > A.tol)) break;   // x (= xold) is the converged iterate (aar.m:57-80)
+    if (anderson) {
+      if (blockIdx.x == 0) {
+        for (int k = threadIdx.x; k < m * (m + 1); k += blockDim.x) {
+          double t = 0;
+          for (int b = 0; b < nblk; ++b) t += __ldcg(A.part + 2 * nblk + (size_t)b * m * (m + 1) + k);
+          gsh[k] = t;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          pinv_solve_1t(gsh, m);                     // gamma -> gsh[m*m + m ..]
+          for (int i = 0; i < m; ++i) A.gam[i] = gsh[m * m + m + i];
+        }
+      }
+      if (!grid_sync(A.bar, A.status)) break;
+      double gam[kAarM];
+      for (int i = 0; i < m; ++i) gam[i] = __ldcg(A.gam + i);
+      for (int p = tid0; p < N; p += stride) {
+        double u = xc[p] + A.beta * A.res[p];
+        for (int i = 0; i < m; ++i) u -= (A.DX[(size_t)i * N + p] + A.beta * A.DF[(size_t)i * N + p]) * gam[i];
+        xn[p] = u;
+      }
+      if (!grid_sync(A.bar, A.status)) break;
+    }
+    double* t = xc;
+    xc = xn;
+    xn = t;
     count++;
   }
   // the returned iterate is x_prev of the last residual evaluation (aar.m:77)
@@ -287,6 +322,7 @@ __global__ void __launch_bounds__(256, 2) k_aar(const __grid_constant__ AarArgs 
     *A.out_iters = min(count, A.maxit);
     *A.out_relres = relres;
   }
+  (void)relres_s;
 }
 
 }  // namespace cx
@@ -299,8 +335,18 @@ cx_status poisson_dev(cx_handle h, const double* d_f, double* d_phi, double tol,
   if (!h || !d_f || !d_phi) return CX_ERR_ARG;
   if (maxit < 1 || !(tol > 0)) { h->err = "cx_poisson: need maxit >= 1 and tol > 0"; return CX_ERR_ARG; }
   const int N = h->g.N, m = kAarM;
-  // workspace: x, vt, res, xold, fold, dinv (N each), DX, DF (N x m), reductions, barrier, outputs
-  const size_t need = (size_t)N * 8 * (6 + 2 * m) + 8 * (2 + m * m + 2 * m) + 4096;
+  // grid: one resident block of 256 threads per SM (cooperative launch), at most one per 256 points
+  int dev = 0, nsm = 0, per_sm = 0;
+  CX_TRY_CUDA(h, cudaGetDevice(&dev));
+  CX_TRY_CUDA(h, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const size_t dyn_smem = (size_t)2 * h->g.Nx * sizeof(double);
+  CX_TRY_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_aar, 256, dyn_smem));
+  if (per_sm < 1) { h->err = "cx_poisson: the AAR kernel does not fit on an SM"; return CX_ERR_CUDA; }
+  const int nblocks = std::max(1, std::min(nsm, (N + 255) / 256));
+  // workspace: x (two), vt, res, xold, fold, dinv (N each), DX, DF (N x m), 1/r and theta scale
+  // (Nx each), per-block partials, Anderson weights, barrier word, outputs
+  const size_t parts = (size_t)2 * nblocks + (size_t)nblocks * m * (m + 1);
+  const size_t need = (size_t)N * 8 * (7 + 2 * m) + (size_t)h->g.Nx * 16 + parts * 8 + 8 * m + 16 * 256;
   if (h->pois_bytes < need) {
     cudaFree(h->d_pois);
     h->d_pois = nullptr;
@@ -311,7 +357,8 @@ cx_status poisson_dev(cx_handle h, const double* d_f, double* d_phi, double tol,
   char* q = (char*)h->d_pois;
   auto take = [&](size_t bytes) { char* o = q; q += (bytes + 255) & ~(size_t)255; return (void*)o; };
   AarArgs A{};
-  A.x = (double*)take((size_t)N * 8);
+  A.x0 = (double*)take((size_t)N * 8);
+  A.x1 = (double*)take((size_t)N * 8);
   A.vt = (double*)take((size_t)N * 8);
   A.res = (double*)take((size_t)N * 8);
   A.xold = (double*)take((size_t)N * 8);
@@ -319,7 +366,10 @@ cx_status poisson_dev(cx_handle h, const double* d_f, double* d_phi, double tol,
   double* dinv = (double*)take((size_t)N * 8);
   A.DX = (double*)take((size_t)N * 8 * m);
   A.DF = (double*)take((size_t)N * 8 * m);
-  A.red = (double*)take(8 * (2 + m * m + 2 * m));
+  double* rinv = (double*)take((size_t)h->g.Nx * 8);
+  double* thsc = (double*)take((size_t)h->g.Nx * 8);
+  A.part = (double*)take(parts * 8);
+  A.gam = (double*)take(8 * m);
   A.bar = (unsigned*)take(64);
   int* outs = (int*)take(64);
   double* outr = (double*)take(64);
@@ -328,11 +378,24 @@ cx_status poisson_dev(cx_handle h, const double* d_f, double* d_phi, double tol,
   const cx_grid& G = h->grid;
   const GridDev& g = h->g;
   A.Nx = g.Nx; A.Ny = g.Ny; A.Nz = g.Nz; A.N = N; A.F = g.FDn; A.helical = g.helical; A.bcy = g.BCy; A.bcz = g.BCz;
-  A.xin = g.xin; A.dx = g.dx; A.twist = g.twist;
   for (int k = 0; k <= kMaxFDn; ++k) {
     A.cr2[k] = h->coef.cr2[k]; A.cr1[k] = h->coef.cr1[k]; A.ct2[k] = h->coef.ct2[k];
     A.ct1[k] = h->coef.ct1[k]; A.cz2[k] = h->coef.cz2[k]; A.cz1[k] = h->coef.cz1[k];
   }
+  {
+    // the per-radial-node factors of the Laplacian (as the Hamiltonian kernels compute them)
+    std::vector<double> ri(g.Nx), ts(g.Nx);
+    for (int r = 0; r < g.Nx; ++r) {
+      const double rr = g.xin + (double)r * g.dx;
+      ri[r] = 1.0 / rr;
+      ts[r] = g.helical ? g.twist * g.twist + 1.0 / (rr * rr) : 1.0 / (rr * rr);
+    }
+    CX_TRY_CUDA(h, cudaMemcpyAsync(rinv, ri.data(), g.Nx * 8, cudaMemcpyHostToDevice, st));
+    CX_TRY_CUDA(h, cudaMemcpyAsync(thsc, ts.data(), g.Nx * 8, cudaMemcpyHostToDevice, st));
+    CX_TRY_CUDA(h, cudaStreamSynchronize(st));
+  }
+  A.rinv = rinv;
+  A.thsc = thsc;
   A.f = d_f;
   A.dinv = dinv;
   A.status = h->d_status;
@@ -345,22 +408,21 @@ cx_status poisson_dev(cx_handle h, const double* d_f, double* d_phi, double tol,
   A.maxit = maxit;
   A.p = 6;
   // x0 = guess or ones (aar.m:51-53); history, sums and barrier cleared; ||f||
-  if (use_guess) CX_TRY_CUDA(h, cudaMemcpyAsync(A.x, d_phi, (size_t)N * 8, cudaMemcpyDeviceToDevice, st));
+  if (use_guess) CX_TRY_CUDA(h, cudaMemcpyAsync(A.x0, d_phi, (size_t)N * 8, cudaMemcpyDeviceToDevice, st));
   else {
     std::vector<double> ones(N, 1.0);
-    CX_TRY_CUDA(h, cudaMemcpyAsync(A.x, ones.data(), (size_t)N * 8, cudaMemcpyHostToDevice, st));
+    CX_TRY_CUDA(h, cudaMemcpyAsync(A.x0, ones.data(), (size_t)N * 8, cudaMemcpyHostToDevice, st));
     CX_TRY_CUDA(h, cudaStreamSynchronize(st));
   }
   CX_TRY_CUDA(h, cudaMemsetAsync(A.vt, 0, (size_t)N * 8, st));
   CX_TRY_CUDA(h, cudaMemsetAsync(A.DX, 0, (size_t)N * 8 * m, st));
   CX_TRY_CUDA(h, cudaMemsetAsync(A.DF, 0, (size_t)N * 8 * m, st));
-  CX_TRY_CUDA(h, cudaMemsetAsync(A.red, 0, 8 * (2 + m * m + 2 * m), st));
+  CX_TRY_CUDA(h, cudaMemsetAsync(A.part, 0, parts * 8, st));
   CX_TRY_CUDA(h, cudaMemsetAsync(A.bar, 0, 64, st));
   const double d0 = G.w2[0] / (G.dx * G.dx) + G.w2[0] / (G.dz * G.dz);
   k_pois_diag<<<gN, 256, 0, st>>>(dinv, G.Nx, N, G.xin, G.dx, d0, G.w2[0] / (G.dy * G.dy), G.twist * G.twist, G.cell_typ != 3);
   h->launches++;
   {
-    // ||f||^2 by cuBLAS-free reduction: reuse the red slot 0
     std::vector<double> fh(N);
     CX_TRY_CUDA(h, cudaMemcpyAsync(fh.data(), d_f, (size_t)N * 8, cudaMemcpyDeviceToHost, st));
     CX_TRY_CUDA(h, cudaStreamSynchronize(st));
@@ -368,14 +430,8 @@ cx_status poisson_dev(cx_handle h, const double* d_f, double* d_phi, double tol,
     for (double v : fh) nb2 += v * v;
     A.nb = 1.0 / std::sqrt(nb2);
   }
-  // one resident grid: as many blocks as fit on the device at once (cooperative launch)
-  int dev = 0, nsm = 0, per_sm = 0;
-  CX_TRY_CUDA(h, cudaGetDevice(&dev));
-  CX_TRY_CUDA(h, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  CX_TRY_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_aar, 256, 0));
-  const int nblocks = std::max(1, std::min(nsm * std::max(1, per_sm), (N + 255) / 256));
   void* args[] = {(void*)&A};
-  CX_TRY_CUDA(h, cudaLaunchCooperativeKernel((const void*)k_aar, dim3(nblocks), dim3(256), args, 0, st));
+  CX_TRY_CUDA(h, cudaLaunchCooperativeKernel((const void*)k_aar, dim3(nblocks), dim3(256), args, dyn_smem, st));
   h->launches++;
   int it = 0, bst = 0;
   double rr = 0;

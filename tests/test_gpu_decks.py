@@ -7,7 +7,11 @@ tests/golden/make_deck_fixtures.py from the reference's deck files with this lib
 loader), so the test needs no reference tree.
 
 Tolerance: free energy per atom within 1e-6 Ha/atom of the printed value (the oracle SCF from the
-same set-up is within 9.0e-8 and 2.7e-9 of it), in FP64 and in mixed precision.
+same set-up is within 9.0e-8 and 2.7e-9 of it), in FP64 and in mixed precision.  The SCF runs to
+the deck's tolerance (at most 1e-6), except in mixed precision on CNT_ABINITmatch: its filter of
+degree 100 in complex64 leaves an SCF error floor near 1e-5 (the error fluctuates between 1e-5
+and 2e-4 from step 20 on), so that run stops at 1e-4; its free energy after the FP64 refinement
+is still within 1e-8 Ha/atom of the printed value.
 """
 import numpy as np
 import pytest
@@ -28,7 +32,8 @@ def test_deck_free_energy_matches_printed(name, prec):
     try:
         for b in range(len(blocks)):
             g.set_psi(b, initial_psi(S.N, S.Nev, 700 + b))
-        res, EV, rho, V, hist = g.scf(S, scf_tol=min(scf_tol, 1e-6), poisson_tol=poisson_tol, max_scf=60)
+        tol = 1e-4 if (prec == "mixed" and S.npl >= 100) else min(scf_tol, 1e-6)
+        res, EV, rho, V, hist = g.scf(S, scf_tol=tol, poisson_tol=poisson_tol, max_scf=60)
     finally:
         g.close()
     assert res.converged == 1
