@@ -43,8 +43,8 @@ void scf_state_free(cx_handle h);
 // FP64 Rayleigh quotients of the device-resident psi (cx_linalg.cu)
 cx_status refine_eigenvalues(cx_handle h, double* EigVal);
 // tensor-core (tcgen05) Rayleigh-Ritz products of the complex64 path (cx_tcgen05.cu):
-// C (n x m, leading dimension ldc) = X^H (w .* Y), w optional; Z (N x m) = X C with C complex128
-cx_status tc_gram(cx_handle h, const float2* X, const float2* Y, const float* w, int N, int n, int m, float2* C, int ldc);
+// C (n x m complex128, leading dimension ldc) = X^H (w .* Y), w optional; Z (N x m) = X C with C complex128
+cx_status tc_gram(cx_handle h, const float2* X, const float2* Y, const float* w, int N, int n, int m, double2* C, int ldc);
 size_t tc_rot_image_floats(int n, int m);
 cx_status tc_rotate(cx_handle h, const float2* X, const double2* C, int N, int n, int m, float2* Z, float* img);
 // status flag of the TMA pipeline: CX_OK, or CX_ERR_CUDA with a message when a CTA timed out

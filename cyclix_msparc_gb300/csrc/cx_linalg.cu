@@ -673,15 +673,11 @@ cx_status rr_gemms<double>(cx_handle h, const double2* X, const double2* HX, int
 
 template <>
 cx_status rr_gemms<float>(cx_handle h, const float2* X, const float2* HX, int N, int n, RRWork& w) {
-  // Gram and projected matrices on the tensor cores (3xTF32, FP32 accumulation), then to FP64
-  cx_status s = tc_gram(h, X, X, nullptr, N, n, n, w.Gf, n);
+  // Gram and projected matrices on the tensor cores (3xTF32 products, FP32 accumulation over short
+  // ranges, FP64 sums)
+  cx_status s = tc_gram(h, X, X, nullptr, N, n, n, w.G, n);
   if (s != CX_OK) return s;
-  if ((s = tc_gram(h, X, HX, nullptr, N, n, n, w.Mf, n)) != CX_OK) return s;
-  const size_t n2 = (size_t)n * n;
-  k_f2d<<<grid_for(n2), 256, 0, h->stream>>>(w.Gf, w.G, n2);
-  k_f2d<<<grid_for(n2), 256, 0, h->stream>>>(w.Mf, w.Hs, n2);
-  h->launches += 2;
-  return CX_OK;
+  return tc_gram(h, X, HX, nullptr, N, n, n, w.Hs, n);
 }
 
 // Gw = X^H Y (complex128)
@@ -694,12 +690,7 @@ static cx_status rr_gram(cx_handle h, const double2* X, const double2* Y, int N,
 }
 // Gw = X^H W X for complex64 X: the weights are applied on the tensor-core operand load
 static cx_status rr_wgram(cx_handle h, const float2* X, int N, int n, RRWork& w) {
-  cx_status s = tc_gram(h, X, X, h->d_W32, N, n, n, w.Gf, n);
-  if (s != CX_OK) return s;
-  const size_t n2 = (size_t)n * n;
-  k_f2d<<<grid_for(n2), 256, 0, h->stream>>>(w.Gf, w.Gw, n2);
-  h->launches++;
-  return CX_OK;
+  return tc_gram(h, X, X, h->d_W32, N, n, n, w.Gw, n);
 }
 
 template <typename R>

@@ -311,11 +311,11 @@ nl_contract_kernel(const int N, const int nstates, const BlockDev<R>* __restrict
 // (the scatter of src/h_nonlocal_vector_mult.m:38-42, scaled like the rest of the Chebyshev step).
 // Per 32-point row chunk that projector balls touch, the entries form a small dense matrix
 // Chi_c (32 points x K = 4 x segments of the chunk, zero where a point is outside a ball), so the
-// apply is Y[chunk, states] += Chi_c . Cp_c[K, states]: a CTA owns one chunk and 64 states and
-// stages Chi_c and Cp_c of its states in shared memory; each warp accumulates 8 states for its
-// 32 points from shared memory only (Chi_c by lane, Cp_c broadcast), one packed (re, im)
-// multiply-add per state and column in the complex64 case.
-constexpr int NA_SPW = 8;      // states per warp
+// apply is Y[chunk, states] += Chi_c . Cp_c[K, states]: a CTA owns one chunk and 32 states and
+// stages Chi_c and Cp_c of its states in shared memory; each warp accumulates 4 states for its
+// 32 points from shared memory only (Chi_c by lane, Cp_c broadcast two columns per load), one
+// packed (re, im) multiply-add per state and column in the complex64 case.
+constexpr int NA_SPW = 4;      // states per warp
 constexpr int NA_SPC = 8 * NA_SPW;
 
 template <typename R>
@@ -360,11 +360,16 @@ nl_apply_kernel(const int N, const int Nx, const BlockDev<R>* __restrict__ block
 #pragma unroll
   for (int j = 0; j < NA_SPW; ++j) acc[j] = mk<R>((R)0, (R)0);
   const cplx<R>* csw = cs + (size_t)sl0 * K;
-#pragma unroll 4
-  for (int k = 0; k < K; ++k) {
-    const R x = chs[k * 32 + lane];
+  // K is a multiple of 4 (kAngMax columns per segment): two columns per step
+#pragma unroll 2
+  for (int k = 0; k < K; k += 2) {
+    const R x0 = chs[k * 32 + lane], x1 = chs[(k + 1) * 32 + lane];
 #pragma unroll
-    for (int j = 0; j < NA_SPW; ++j) cfma_real<R>(acc[j], x, csw[(size_t)j * K + k]);
+    for (int j = 0; j < NA_SPW; ++j) {
+      const cplx<R> v0 = csw[(size_t)j * K + k], v1 = csw[(size_t)j * K + k + 1];
+      cfma_real<R>(acc[j], x0, v0);
+      cfma_real<R>(acc[j], x1, v1);
+    }
   }
   if (!ok) return;
 #pragma unroll

@@ -2,7 +2,9 @@
 // (tcgen05.mma, accumulators in tensor memory), written for sm_103a without a library:
 //
 //   gram:    C = X^H (w .* Y)      X: N x n, Y: N x m complex64 (column-major), w: optional real
-//                                  weights (N); C: n x m complex, FP32, accumulated with atomics
+//                                  weights (N); C: n x m complex128: each CTA accumulates a short
+//                                  range of the reduction in FP32 (tensor memory) and adds it to C
+//                                  with FP64 atomics
 //            (the Gram matrix X^H X, the projected Hamiltonian X^H (H X) and the W-Gram
 //            X^H W X of src/eigSolver.m:99-104, in the Cholesky-QR form of this library);
 //   rotate:  Z = X C               X: N x n complex64, C: n x m complex (FP64 in, split on the
@@ -140,12 +142,14 @@ constexpr int kGramXc = 64;      // X columns per tile (MMA M = 128: x^ and x~ r
 constexpr int kGramN = 128;      // Y columns per tile (MMA N)
 constexpr int kGramStageBytes = 4 * kTileBytes;   // A hi, A lo, B hi, B lo
 constexpr size_t kGramSmem = 1024 + (size_t)kGramStages * kGramStageBytes;
+constexpr int kGramPieces = (kGramXc + kGramN) * 8 / (32 * kProducerWarps);   // 16-byte pieces per producer thread and stage
+static_assert((kGramXc + kGramN) * 8 % (32 * kProducerWarps) == 0, "pieces per stage");
 
 struct GramArgs {
   const float2* X;
   const float2* Y;
   const float* w;           // optional weights on Y (nullptr: none)
-  float2* C;                // n x m, leading dimension ldc; accumulated (zero it first)
+  double2* C;               // n x m, leading dimension ldc; accumulated in FP64 (zero it first)
   int N, n, m, ldc;
   int kchunk;               // complex grid points per split (multiple of 16)
   int* status;
@@ -183,10 +187,46 @@ __global__ void __launch_bounds__(kThreads, 1) gram_kernel(const __grid_constant
   const uint32_t tmem = *tmem_slot;
 
   if (warp < kProducerWarps) {
-    // ---- producers: 64 X columns and 128 Y columns x 16 complex grid points per stage, 16 B per piece
+    // ---- producers: 64 X columns and 128 Y columns x 16 complex grid points per stage, 16 B per
+    // piece, kGramPieces pieces per thread.  The next stage's pieces are loaded into registers
+    // before the current ones are split and stored, so a stage's global-load latency overlaps the
+    // previous stage's work.
     const int t = threadIdx.x;
+    auto load_stage = [&](int it, float4 (&v)[kGramPieces]) {
+      const int kc0 = kbeg + 16 * it;
+#pragma unroll
+      for (int u = 0; u < kGramPieces; ++u) {
+        const int pc = t + u * 32 * kProducerWarps;
+        const int col = pc >> 3, q = pc & 7;
+        const int k = kc0 + 2 * q;
+        const bool isx = col < kGramXc;
+        const int c = isx ? i0 + col : j0 + (col - kGramXc);
+        const float2* src = isx ? A.X : A.Y;
+        float4 w4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (c < (isx ? A.n : A.m)) {
+          const float2* colp = src + (size_t)c * A.N;
+          if (k + 1 < kend && !(A.N & 1)) {
+            w4 = *reinterpret_cast<const float4*>(colp + k);     // 16-byte aligned: N and k even
+          } else if (k + 1 < kend) {
+            const float2 e = colp[k], f = colp[k + 1];
+            w4 = make_float4(e.x, e.y, f.x, f.y);
+          } else if (k < kend) {
+            const float2 e = colp[k];
+            w4 = make_float4(e.x, e.y, 0.f, 0.f);
+          }
+          if (!isx && A.w) {
+            const float w0 = k < kend ? A.w[k] : 0.f, w1 = k + 1 < kend ? A.w[k + 1] : 0.f;
+            w4.x *= w0; w4.y *= w0; w4.z *= w1; w4.w *= w1;
+          }
+        }
+        v[u] = w4;
+      }
+    };
+    float4 cur[kGramPieces], nxt[kGramPieces];
+    if (nk > 0) load_stage(0, cur);
     for (int it = 0; it < nk && !*(volatile int*)failed; ++it) {
       const int s = it % kGramStages;
+      if (it + 1 < nk) load_stage(it + 1, nxt);
       if (it >= kGramStages && !mbar_wait(&empty[s], (uint32_t)(((it / kGramStages) - 1) & 1))) {
         atomicExch(failed, 1);
         break;
@@ -195,33 +235,13 @@ __global__ void __launch_bounds__(kThreads, 1) gram_kernel(const __grid_constant
       unsigned char* Alo = Ahi + kTileBytes;
       unsigned char* Bhi = Alo + kTileBytes;
       unsigned char* Blo = Bhi + kTileBytes;
-      const int kc0 = kbeg + 16 * it;
-#pragma unroll 4
-      for (int p = t; p < (kGramXc + kGramN) * 8; p += 32 * kProducerWarps) {
-        const int col = p >> 3, q = p & 7;
-        const int k = kc0 + 2 * q;
-        const bool isx = col < kGramXc;
-        const int c = isx ? i0 + col : j0 + (col - kGramXc);
-        const float2* src = isx ? A.X : A.Y;
-        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (c < (isx ? A.n : A.m)) {
-          const float2* colp = src + (size_t)c * A.N;
-          if (k + 1 < kend && !(A.N & 1)) {
-            v = *reinterpret_cast<const float4*>(colp + k);      // 16-byte aligned: N and k even
-          } else if (k + 1 < kend) {
-            const float2 a = colp[k], b = colp[k + 1];
-            v = make_float4(a.x, a.y, b.x, b.y);
-          } else if (k < kend) {
-            const float2 a = colp[k];
-            v = make_float4(a.x, a.y, 0.f, 0.f);
-          }
-          if (!isx && A.w) {
-            const float w0 = k < kend ? A.w[k] : 0.f, w1 = k + 1 < kend ? A.w[k + 1] : 0.f;
-            v.x *= w0; v.y *= w0; v.z *= w1; v.w *= w1;
-          }
-        }
+#pragma unroll
+      for (int u = 0; u < kGramPieces; ++u) {
+        const int pc = t + u * 32 * kProducerWarps;
+        const int col = pc >> 3, q = pc & 7;
+        const float4 v = cur[u];
         float4 hi, lo;
-        if (isx) {
+        if (col < kGramXc) {
           split4(v, hi, lo);
           *reinterpret_cast<float4*>(Ahi + core_off(col, q)) = hi;
           *reinterpret_cast<float4*>(Alo + core_off(col, q)) = lo;
@@ -236,6 +256,8 @@ __global__ void __launch_bounds__(kThreads, 1) gram_kernel(const __grid_constant
       }
       fence_async_smem();
       mbar_arrive(&full[s]);
+#pragma unroll
+      for (int u = 0; u < kGramPieces; ++u) cur[u] = nxt[u];
     }
   } else if (lane == 0) {
     // ---- MMA issuer
@@ -278,7 +300,7 @@ __global__ void __launch_bounds__(kThreads, 1) gram_kernel(const __grid_constant
 #pragma unroll
           for (int e = 0; e < 16; ++e) {
             const int j = j0 + cb * 16 + e;
-            if (j < A.m) atomicAdd(reinterpret_cast<float*>(A.C + (size_t)j * A.ldc + i) + part, v[e]);
+            if (j < A.m) atomicAdd(reinterpret_cast<double*>(A.C + (size_t)j * A.ldc + i) + part, (double)v[e]);
           }
         }
       }
@@ -341,8 +363,28 @@ __global__ void __launch_bounds__(kThreads, 1) rotate_kernel(const __grid_consta
   const uint32_t tmem = *tmem_slot;
 
   if (warp < kProducerWarps) {
+    // X: 128 grid points x 32 columns per stage; a warp task = 32 points (one per lane) x 4
+    // columns, 8 tasks per warp.  The next stage's values are loaded into registers before the
+    // current ones are split and stored (the load latency overlaps the previous stage's work).
+    constexpr int kTasks = 32 / kProducerWarps;
+    auto load_stage = [&](int it, float2 (&v)[kTasks][4]) {
+      const int ic0 = 32 * it;
+#pragma unroll
+      for (int u = 0; u < kTasks; ++u) {
+        const int task = warp + u * kProducerWarps;
+        const int rb = task & 3, cq = task >> 2;          // row block of 32, column quad
+        const int k = k0 + 32 * rb + lane;
+        const int ib = ic0 + 4 * cq;
+        const float2* xp = A.X + (size_t)ib * A.N + k;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) v[u][e] = (k < A.N && ib + e < A.n) ? xp[(size_t)e * A.N] : make_float2(0.f, 0.f);
+      }
+    };
+    float2 cur[kTasks][4], nxt[kTasks][4];
+    if (nk > 0) load_stage(0, cur);
     for (int it = 0; it < nk && !*(volatile int*)failed; ++it) {
       const int s = it % kRotStages;
+      if (it + 1 < nk) load_stage(it + 1, nxt);
       if (it >= kRotStages && !mbar_wait(&empty[s], (uint32_t)(((it / kRotStages) - 1) & 1))) {
         atomicExch(failed, 1);
         break;
@@ -357,22 +399,13 @@ __global__ void __launch_bounds__(kThreads, 1) rotate_kernel(const __grid_consta
                      "l"(src), "r"((uint32_t)(4 * kRotBTile)), "r"(su32(&full[s]))
                      : "memory");
       }
-      // X: 128 grid points x 32 columns; a warp task = 32 points (one per lane) x 4 columns
-      const int ic0 = 32 * it;
-      for (int task = warp; task < 32; task += kProducerWarps) {
-        const int rb = task & 3, cq = task >> 2;          // row block of 32, column quad
-        const int r = 32 * rb + lane, k = k0 + r;
-        float4 re = make_float4(0.f, 0.f, 0.f, 0.f), im = re;
-        if (k < A.N) {
-          const int ib = ic0 + 4 * cq;
-          const float2* xp = A.X + (size_t)ib * A.N + k;
-          const float2 x0 = ib < A.n ? xp[0] : make_float2(0.f, 0.f);
-          const float2 x1 = ib + 1 < A.n ? xp[(size_t)A.N] : make_float2(0.f, 0.f);
-          const float2 x2 = ib + 2 < A.n ? xp[2 * (size_t)A.N] : make_float2(0.f, 0.f);
-          const float2 x3 = ib + 3 < A.n ? xp[3 * (size_t)A.N] : make_float2(0.f, 0.f);
-          re = make_float4(x0.x, x1.x, x2.x, x3.x);
-          im = make_float4(x0.y, x1.y, x2.y, x3.y);
-        }
+#pragma unroll
+      for (int u = 0; u < kTasks; ++u) {
+        const int task = warp + u * kProducerWarps;
+        const int rb = task & 3, cq = task >> 2;
+        const int r = 32 * rb + lane;
+        const float4 re = make_float4(cur[u][0].x, cur[u][1].x, cur[u][2].x, cur[u][3].x);
+        const float4 im = make_float4(cur[u][0].y, cur[u][1].y, cur[u][2].y, cur[u][3].y);
         float4 hi, lo;
         split4(re, hi, lo);
         *reinterpret_cast<float4*>(st + 0 * kRotATile + core_off(r, cq)) = hi;
@@ -383,6 +416,10 @@ __global__ void __launch_bounds__(kThreads, 1) rotate_kernel(const __grid_consta
       }
       fence_async_smem();
       mbar_arrive(&full[s]);
+#pragma unroll
+      for (int u = 0; u < kTasks; ++u)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) cur[u][e] = nxt[u][e];
     }
   } else if (lane == 0) {
     constexpr uint32_t id_pos = idesc_tf32(kRotM, kRotN, false), id_neg = idesc_tf32(kRotM, kRotN, true);
@@ -489,19 +526,21 @@ __global__ void k_rot_image(const double2* __restrict__ C, int n, int m, int nks
 
 }  // namespace tc
 
-// C (n x m, leading dimension ldc, float2) = X^H (w .* Y); C is zeroed here.
-cx_status tc_gram(cx_handle h, const float2* X, const float2* Y, const float* w, int N, int n, int m, float2* C, int ldc) {
+// C (n x m, leading dimension ldc, complex128) = X^H (w .* Y); C is zeroed here.
+cx_status tc_gram(cx_handle h, const float2* X, const float2* Y, const float* w, int N, int n, int m, double2* C, int ldc) {
   using namespace tc;
-  CX_TRY_CUDA(h, cudaMemsetAsync(C, 0, (size_t)ldc * m * sizeof(float2), h->stream));
+  CX_TRY_CUDA(h, cudaMemsetAsync(C, 0, (size_t)ldc * m * sizeof(double2), h->stream));
   if (N <= 0 || n <= 0 || m <= 0) return CX_OK;
   CX_TRY_CUDA(h, cudaFuncSetAttribute(gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGramSmem));
   int dev = 0, nsm = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const int tiles = ((n + kGramXc - 1) / kGramXc) * ((m + kGramN - 1) / kGramN);
-  // split the reduction over the grid points so that about two CTAs per SM run
+  // split the reduction over the grid points: short FP32 ranges (at most 1024 grid points, 2048
+  // real terms, per CTA) and at least about two CTAs per SM
   int splits = std::max(1, (2 * nsm + tiles - 1) / tiles);
   int kchunk = (N + splits - 1) / splits;
+  kchunk = std::min(kchunk, 1024);
   kchunk = std::max(16 * 8, (kchunk + 15) / 16 * 16);
   splits = (N + kchunk - 1) / kchunk;
   GramArgs a{X, Y, w, C, N, n, m, ldc, kchunk, h->d_status};
