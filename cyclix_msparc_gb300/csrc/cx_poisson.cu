@@ -30,59 +30,89 @@ __global__ void k_pois_diag(double* dinv, int Nx, int N, double xin, double dx, 
   }
 }
 
-// gamma = pinv(A) v for the symmetric m x m A in io (A row-major, then v; gamma written after v):
-// cyclic Jacobi eigen-decomposition by one thread, MATLAB's pinv tolerance
-__device__ __noinline__ void pinv_solve_1t(double* __restrict__ io, int m) {
-  double A[kAarM][kAarM], V[kAarM][kAarM], v[kAarM];
-  for (int i = 0; i < m; ++i) {
-    v[i] = io[m * m + i];
-    for (int j = 0; j < m; ++j) { A[i][j] = io[i * m + j]; V[i][j] = i == j ? 1.0 : 0.0; }
+// gamma = pinv(A) v for the symmetric kAarM x kAarM A in io (A row-major, then v; gamma written
+// after v): cyclic Jacobi eigen-decomposition by one thread with MATLAB's pinv tolerance.  The
+// matrices live in registers (every index is a compile-time constant); each rotation sets its
+// pair exactly to zero, a pair below rounding of its diagonal is dropped, and the sweeps stop once
+// the off-diagonal mass is below 1e-36 of the total (quadratic convergence: a handful of sweeps).
+__device__ __noinline__ void pinv_solve_1t(double* __restrict__ io) {
+  constexpr int M = kAarM;
+  double A[M][M], V[M][M], v[M];
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+    v[i] = io[M * M + i];
+#pragma unroll
+    for (int j = 0; j < M; ++j) { A[i][j] = io[i * M + j]; V[i][j] = i == j ? 1.0 : 0.0; }
   }
-  for (int sweep = 0; sweep < 60; ++sweep) {
-    double off = 0;
-    for (int i = 0; i < m; ++i) for (int j = i + 1; j < m; ++j) off += A[i][j] * A[i][j];
-    if (off < 1e-300) break;
-    for (int p = 0; p < m; ++p) {
-      for (int q = p + 1; q < m; ++q) {
-        if (fabs(A[p][q]) < 1e-300) continue;
-        const double th = (A[q][q] - A[p][p]) / (2 * A[p][q]);
-        const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1));
-        const double c = 1 / sqrt(t * t + 1), s = t * c;
-        for (int k = 0; k < m; ++k) {
-          const double akp = A[k][p], akq = A[k][q];
-          A[k][p] = c * akp - s * akq;
-          A[k][q] = s * akp + c * akq;
-        }
-        for (int k = 0; k < m; ++k) {
-          const double apk = A[p][k], aqk = A[q][k];
-          A[p][k] = c * apk - s * aqk;
-          A[q][k] = s * apk + c * aqk;
-        }
-        for (int k = 0; k < m; ++k) {
-          const double vkp = V[k][p], vkq = V[k][q];
-          V[k][p] = c * vkp - s * vkq;
-          V[k][q] = s * vkp + c * vkq;
+  for (int sweep = 0; sweep < 40; ++sweep) {
+    double off = 0, tot = 0;
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+      tot += A[i][i] * A[i][i];
+#pragma unroll
+      for (int j = i + 1; j < M; ++j) off += A[i][j] * A[i][j];
+    }
+    if (!(off > 1.0e-36 * (tot + 2 * off))) break;
+#pragma unroll
+    for (int p = 0; p < M; ++p) {
+#pragma unroll
+      for (int q = p + 1; q < M; ++q) {
+        const double apq = A[p][q];
+        if (fabs(apq) <= 1.0e-18 * (fabs(A[p][p]) + fabs(A[q][q]))) {
+          A[p][q] = 0.0;   // below rounding of the diagonal: drop it
+          A[q][p] = 0.0;
+        } else {
+          const double th = (A[q][q] - A[p][p]) / (2 * apq);
+          const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1));
+          const double c = 1 / sqrt(t * t + 1), s = t * c;
+#pragma unroll
+          for (int k = 0; k < M; ++k) {
+            const double akp = A[k][p], akq = A[k][q];
+            A[k][p] = c * akp - s * akq;
+            A[k][q] = s * akp + c * akq;
+          }
+#pragma unroll
+          for (int k = 0; k < M; ++k) {
+            const double apk = A[p][k], aqk = A[q][k];
+            A[p][k] = c * apk - s * aqk;
+            A[q][k] = s * apk + c * aqk;
+          }
+          A[p][q] = 0.0;
+          A[q][p] = 0.0;
+#pragma unroll
+          for (int k = 0; k < M; ++k) {
+            const double vkp = V[k][p], vkq = V[k][q];
+            V[k][p] = c * vkp - s * vkq;
+            V[k][q] = s * vkp + c * vkq;
+          }
         }
       }
     }
   }
   double nrm = 0;
-  for (int i = 0; i < m; ++i) nrm = fmax(nrm, fabs(A[i][i]));
-  const double tol = m * nrm * 2.220446049250313e-16;   // MATLAB pinv: max(size(A)) * norm(A) * eps
-  double g[kAarM];
-  for (int i = 0; i < m; ++i) g[i] = 0;
-  for (int k = 0; k < m; ++k) {
-    if (fabs(A[k][k]) <= tol) continue;
-    double c = 0;
-    for (int i = 0; i < m; ++i) c += V[i][k] * v[i];
-    c /= A[k][k];
-    for (int i = 0; i < m; ++i) g[i] += V[i][k] * c;
+#pragma unroll
+  for (int i = 0; i < M; ++i) nrm = fmax(nrm, fabs(A[i][i]));
+  const double tol = M * nrm * 2.220446049250313e-16;   // MATLAB pinv: max(size(A)) * norm(A) * eps
+  double g[M];
+#pragma unroll
+  for (int i = 0; i < M; ++i) g[i] = 0;
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    if (fabs(A[k][k]) > tol) {
+      double c = 0;
+#pragma unroll
+      for (int i = 0; i < M; ++i) c += V[i][k] * v[i];
+      c /= A[k][k];
+#pragma unroll
+      for (int i = 0; i < M; ++i) g[i] += V[i][k] * c;
+    }
   }
-  for (int i = 0; i < m; ++i) io[m * m + m + i] = g[i];
+#pragma unroll
+  for (int i = 0; i < M; ++i) io[M * M + M + i] = g[i];
 }
 
-__global__ void k_pois_pinv(double* __restrict__ io, int m) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) pinv_solve_1t(io, m);
+__global__ void k_pois_pinv(double* __restrict__ io) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) pinv_solve_1t(io);
 }
 
 // ---------------------------------------------------------------------------- persistent AAR
@@ -297,7 +327,7 @@ __global__ void __launch_bounds__(256, 2) k_aar(const __grid_constant__ AarArgs 
         }
         __syncthreads();
         if (threadIdx.x == 0) {
-          pinv_solve_1t(gsh, m);                     // gamma -> gsh[m*m + m ..]
+          pinv_solve_1t(gsh);                        // gamma -> gsh[m*m + m ..]
           for (int i = 0; i < m; ++i) A.gam[i] = gsh[m * m + m + i];
         }
       }
@@ -453,9 +483,11 @@ cx_status poisson_dev(cx_handle h, const double* d_f, double* d_phi, double tol,
   return CX_OK;
 }
 
-// gamma = pinv(A) v for an m x m symmetric A, on the device (io layout of k_pois_pinv)
+// gamma = pinv(A) v for an m x m symmetric A, on the device (io layout of k_pois_pinv; m = 7, the
+// AAR and Pulay history length)
 cudaError_t launch_pinv_solve(double* io, int m, cudaStream_t st) {
-  k_pois_pinv<<<1, 32, 0, st>>>(io, m);
+  if (m != kAarM) return cudaErrorInvalidValue;
+  k_pois_pinv<<<1, 32, 0, st>>>(io);
   return cudaGetLastError();
 }
 

@@ -311,22 +311,11 @@ nl_contract_kernel(const int N, const int nstates, const BlockDev<R>* __restrict
 // (the scatter of src/h_nonlocal_vector_mult.m:38-42, scaled like the rest of the Chebyshev step).
 // Per 32-point row chunk that projector balls touch, the entries form a small dense matrix
 // Chi_c (32 points x K = 4 x segments of the chunk, zero where a point is outside a ball), so the
-// apply is Y[chunk, states] += Chi_c . Cp_c[K, states]: a CTA owns one chunk and 32 states and
-// stages Chi_c and Cp_c of its states in shared memory; each warp accumulates 4 states for its
-// 32 points from shared memory only (Chi_c by lane, Cp_c broadcast two columns per load), one
-// packed (re, im) multiply-add per state and column in the complex64 case.
+// apply is Y[chunk, states] += Chi_c . Cp_c[K, states]: a CTA owns one chunk and 32 states, stages
+// Cp_c of its states in shared memory, and each warp accumulates 4 states for its 32 points with
+// coalesced Chi_c loads and broadcast shared-memory reads.
 constexpr int NA_SPW = 4;      // states per warp
 constexpr int NA_SPC = 8 * NA_SPW;
-
-template <typename R>
-__device__ __forceinline__ void cfma_real(cplx<R>& acc, R x, cplx<R> v) {
-  acc.x = fma(x, v.x, acc.x);
-  acc.y = fma(x, v.y, acc.y);
-}
-template <>
-__device__ __forceinline__ void cfma_real<float>(float2& acc, float x, float2 v) {
-  acc = __ffma2_rn(make_float2(x, x), v, acc);
-}
 
 template <typename R>
 __global__ void __launch_bounds__(256)
@@ -334,12 +323,11 @@ nl_apply_kernel(const int N, const int Nx, const BlockDev<R>* __restrict__ block
                 const int2* __restrict__ state_tab, const int nstates, const int out_sel, const ChunkTables ct,
                 const cplx<R>* __restrict__ cprime, const int nseg) {
   extern __shared__ __align__(16) unsigned char nl_smem[];
+  cplx<R>* cs = (cplx<R>*)nl_smem;                       // [NA_SPC][K]
   const int c = blockIdx.x;
   const int p0 = ct.p0[c];
   const int sb = ct.seg_ptr[c], nsc = ct.seg_ptr[c + 1] - sb;
   const int K = nsc * kAngMax;
-  cplx<R>* cs = (cplx<R>*)nl_smem;                       // [NA_SPC][K]
-  R* chs = (R*)(cs + (size_t)NA_SPC * K);                // [K][32]
   const int gsb = blockIdx.y * NA_SPC;
   const int nst_cta = min(NA_SPC, nstates - gsb);
   for (int i = threadIdx.x; i < nst_cta * K; i += blockDim.x) {
@@ -347,8 +335,6 @@ nl_apply_kernel(const int N, const int Nx, const BlockDev<R>* __restrict__ block
     const int sg = ct.segs[sb + k / kAngMax];
     cs[i] = cprime[((size_t)(gsb + sl) * nseg + sg) * kAngMax + (k % kAngMax)];
   }
-  const R* __restrict__ chi_g = (const R*)ct.chi + ct.chi_ptr[c];
-  for (int i = threadIdx.x; i < K * 32; i += blockDim.x) chs[i] = chi_g[i];
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int sl0 = w * NA_SPW;
@@ -356,19 +342,17 @@ nl_apply_kernel(const int N, const int Nx, const BlockDev<R>* __restrict__ block
   const int nst = min(NA_SPW, nst_cta - sl0);
   const int r = p0 % Nx + lane;
   const bool ok = r < Nx;
+  const R* __restrict__ chi = (const R*)ct.chi + ct.chi_ptr[c] + lane;     // [K][32]
   cplx<R> acc[NA_SPW];
 #pragma unroll
   for (int j = 0; j < NA_SPW; ++j) acc[j] = mk<R>((R)0, (R)0);
-  const cplx<R>* csw = cs + (size_t)sl0 * K;
-  // K is a multiple of 4 (kAngMax columns per segment): two columns per step
-#pragma unroll 2
-  for (int k = 0; k < K; k += 2) {
-    const R x0 = chs[k * 32 + lane], x1 = chs[(k + 1) * 32 + lane];
+  for (int k = 0; k < K; ++k) {
+    const R x = chi[(size_t)k * 32];
 #pragma unroll
     for (int j = 0; j < NA_SPW; ++j) {
-      const cplx<R> v0 = csw[(size_t)j * K + k], v1 = csw[(size_t)j * K + k + 1];
-      cfma_real<R>(acc[j], x0, v0);
-      cfma_real<R>(acc[j], x1, v1);
+      const cplx<R> v = cs[(sl0 + j) * K + k];
+      acc[j].x = fma(x, v.x, acc[j].x);
+      acc[j].y = fma(x, v.y, acc[j].y);
     }
   }
   if (!ok) return;
@@ -392,7 +376,7 @@ cudaError_t launch_nl_apply(const GridDev& g, const BlockDev<R>* blocks, const S
   if (ct.nchunks == 0 || nseg == 0) return cudaSuccess;
   dim3 grid((unsigned)ct.nchunks, (unsigned)((nstates + NA_SPC - 1) / NA_SPC));
   if (grid.y > 65535) return cudaErrorInvalidConfiguration;
-  const size_t smem = (size_t)NA_SPC * ct.kmax * sizeof(cplx<R>) + (size_t)ct.kmax * 32 * sizeof(R);
+  const size_t smem = (size_t)NA_SPC * ct.kmax * sizeof(cplx<R>);
   if (smem > 48 * 1024) {
     if (smem > 200 * 1024) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(nl_apply_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

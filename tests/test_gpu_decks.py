@@ -39,5 +39,7 @@ def test_deck_free_energy_matches_printed(name, prec):
     assert res.converged == 1
     e = res.Etotal / S.n_atm
     assert abs(e - e_ref) < 1e-6, (name, prec, e, e_ref)
-    # the electron count is conserved
-    assert abs(float(np.sum(rho * S.W)) + S.NegCharge) < 1e-8 * abs(S.NegCharge)
+    # the electron count is conserved: to rounding in FP64; in mixed precision the density is
+    # summed from complex64 states, whose W-norms carry FP32 rounding (measured 1.0e-8 relative)
+    ctol = 1e-8 if prec == "fp64" else 1e-6
+    assert abs(float(np.sum(rho * S.W)) + S.NegCharge) < ctol * abs(S.NegCharge)
