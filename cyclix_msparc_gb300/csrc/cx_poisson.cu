@@ -4,7 +4,7 @@
 // with real coefficients (k = 0) and the boundary conditions of the grid.
 // The reference preconditions with ILU(1e-5) (src/initialization.m:752); here the diagonal of
 // Lap_std (Jacobi) is used, which keeps every step a streaming pass.  The Anderson least-squares
-// step pinv(DF'DF) (DF' res) (aar.m:74) is solved on the device by a one-thread Jacobi
+// step pinv(DF'DF) (DF' res) (aar.m:74) is solved on the device by a one-warp Jacobi
 // eigen-decomposition of the m x m normal matrix with MATLAB's pinv tolerance.
 //
 // The whole iteration runs in one persistent cooperative kernel: its vectors (a few MB, the
@@ -31,88 +31,112 @@ __global__ void k_pois_diag(double* dinv, int Nx, int N, double xin, double dx, 
 }
 
 // gamma = pinv(A) v for the symmetric kAarM x kAarM A in io (A row-major, then v; gamma written
-// after v): cyclic Jacobi eigen-decomposition by one thread with MATLAB's pinv tolerance.  The
-// matrices live in registers (every index is a compile-time constant); each rotation sets its
-// pair exactly to zero, a pair below rounding of its diagonal is dropped, and the sweeps stop once
-// the off-diagonal mass is below 1e-36 of the total (quadratic convergence: a handful of sweeps).
-__device__ __noinline__ void pinv_solve_1t(double* __restrict__ io) {
-  constexpr int M = kAarM;
-  double A[M][M], V[M][M], v[M];
-#pragma unroll
-  for (int i = 0; i < M; ++i) {
-    v[i] = io[M * M + i];
-#pragma unroll
-    for (int j = 0; j < M; ++j) { A[i][j] = io[i * M + j]; V[i][j] = i == j ? 1.0 : 0.0; }
+// after v), MATLAB's pinv tolerance (aar.m:74, mixing.m:104), by one warp.  Jacobi
+// eigen-decomposition A = V diag(lambda) V^T in the parallel (round-robin) ordering: the 7
+// indices plus a dummy form 4 disjoint pairs per round, 7 rounds per sweep, so the 3 real
+// rotations of a round are computed side by side and applied together as A <- J^T A J,
+// V <- V J (lane L updates entries L and L + 32 of the 8 x 8 arrays in shared memory).  A pair is
+// rotated while |a_pq| > 1e-15 sqrt(|a_pp a_qq|) (the relative criterion for positive
+// semi-definite matrices) and set exactly to zero after its rotation; the sweeps end when a sweep
+// rotates nothing (at most 30).  Then gamma = sum over |lambda_k| > 7 max|lambda| eps of
+// V_k (V_k . v) / lambda_k.  The whole warp must call it; sA, sV are 64 doubles each, cs 4 x 4.
+__device__ __noinline__ void pinv_solve_warp(double* __restrict__ io, double* __restrict__ sA, double* __restrict__ sV,
+                                             double* __restrict__ cs) {
+  constexpr int M = kAarM, P = 8;
+  static_assert(M < P, "one dummy index");
+  const int lane = threadIdx.x & 31;
+  for (int e = lane; e < P * P; e += 32) {
+    const int i = e / P, j = e % P;
+    sA[e] = (i < M && j < M) ? io[i * M + j] : 0.0;
+    sV[e] = i == j ? 1.0 : 0.0;
   }
-  for (int sweep = 0; sweep < 40; ++sweep) {
-    double off = 0, tot = 0;
-#pragma unroll
-    for (int i = 0; i < M; ++i) {
-      tot += A[i][i] * A[i][i];
-#pragma unroll
-      for (int j = i + 1; j < M; ++j) off += A[i][j] * A[i][j];
-    }
-    if (!(off > 1.0e-36 * (tot + 2 * off))) break;
-#pragma unroll
-    for (int p = 0; p < M; ++p) {
-#pragma unroll
-      for (int q = p + 1; q < M; ++q) {
-        const double apq = A[p][q];
-        if (fabs(apq) <= 1.0e-18 * (fabs(A[p][p]) + fabs(A[q][q]))) {
-          A[p][q] = 0.0;   // below rounding of the diagonal: drop it
-          A[q][p] = 0.0;
-        } else {
-          const double th = (A[q][q] - A[p][p]) / (2 * apq);
-          const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1));
-          const double c = 1 / sqrt(t * t + 1), s = t * c;
-#pragma unroll
-          for (int k = 0; k < M; ++k) {
-            const double akp = A[k][p], akq = A[k][q];
-            A[k][p] = c * akp - s * akq;
-            A[k][q] = s * akp + c * akq;
-          }
-#pragma unroll
-          for (int k = 0; k < M; ++k) {
-            const double apk = A[p][k], aqk = A[q][k];
-            A[p][k] = c * apk - s * aqk;
-            A[q][k] = s * apk + c * aqk;
-          }
-          A[p][q] = 0.0;
-          A[q][p] = 0.0;
-#pragma unroll
-          for (int k = 0; k < M; ++k) {
-            const double vkp = V[k][p], vkq = V[k][q];
-            V[k][p] = c * vkp - s * vkq;
-            V[k][q] = s * vkp + c * vkq;
+  __syncwarp();
+  for (int sweep = 0; sweep < 30; ++sweep) {
+    bool rotated = false;
+    for (int rnd = 0; rnd < P - 1; ++rnd) {
+      // pair k of this round: k = 0 is (7, rnd), k = 1..3 are ((rnd + k) % 7, (rnd - k + 7) % 7)
+      if (lane < 4) {
+        int p = lane == 0 ? P - 1 : (rnd + lane) % (P - 1), q = lane == 0 ? rnd : (rnd - lane + P - 1) % (P - 1);
+        if (p > q) { const int t = p; p = q; q = t; }
+        double c = 1.0, sn = 0.0, on = 0.0;
+        if (q < M) {
+          const double app = sA[p * P + p], aqq = sA[q * P + q], apq = sA[p * P + q];
+          if (fabs(apq) > 1e-300 && fabs(apq) > 1e-15 * sqrt(fabs(app * aqq))) {
+            const double th = (aqq - app) / (2 * apq);
+            const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1));
+            c = 1 / sqrt(t * t + 1);
+            sn = t * c;
+            on = 1.0;
           }
         }
+        cs[lane * 4 + 0] = c;
+        cs[lane * 4 + 1] = sn;
+        cs[lane * 4 + 2] = on;
+        cs[lane * 4 + 3] = (double)(p * P + q);
+      }
+      __syncwarp();
+      const bool any = cs[2] + cs[6] + cs[10] + cs[14] > 0;
+      if (any) {
+        rotated = true;
+        // per index i: partner pi, factors (ci, si) with column i of A J = ci col_i + si col_pi
+        auto fac = [&](int i, int& pi, double& ci, double& si) {
+          pi = i; ci = 1.0; si = 0.0;
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const int pq = (int)cs[k * 4 + 3], p = pq / P, q = pq % P;
+            if (cs[k * 4 + 2] > 0 && (i == p || i == q)) {
+              pi = i == p ? q : p;
+              ci = cs[k * 4 + 0];
+              si = i == p ? -cs[k * 4 + 1] : cs[k * 4 + 1];
+            }
+          }
+        };
+        double na[2], nv[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int e = lane + 32 * h, i = e / P, j = e % P;
+          int pi, pj;
+          double ci, si, cj, sj;
+          fac(i, pi, ci, si);
+          fac(j, pj, cj, sj);
+          na[h] = ci * cj * sA[i * P + j] + ci * sj * sA[i * P + pj] + si * cj * sA[pi * P + j] + si * sj * sA[pi * P + pj];
+          if ((pi == j && i != j)) na[h] = 0.0;   // the rotated pair itself
+          nv[h] = sV[i * P + j] * cj + sV[i * P + pj] * sj;   // (V J)[i][j]
+        }
+        __syncwarp();
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          sA[lane + 32 * h] = na[h];
+          sV[lane + 32 * h] = nv[h];
+        }
+      }
+      __syncwarp();
+    }
+    if (!rotated) break;
+  }
+  if (lane == 0) {
+    double nrm = 0;
+    for (int i = 0; i < M; ++i) nrm = fmax(nrm, fabs(sA[i * P + i]));
+    const double tol = M * nrm * 2.220446049250313e-16;   // MATLAB pinv: max(size(A)) * norm(A) * eps
+    double g[M];
+    for (int i = 0; i < M; ++i) g[i] = 0;
+    for (int k = 0; k < M; ++k) {
+      const double lk = sA[k * P + k];
+      if (fabs(lk) > tol) {
+        double c = 0;
+        for (int i = 0; i < M; ++i) c += sV[i * P + k] * io[M * M + i];
+        c /= lk;
+        for (int i = 0; i < M; ++i) g[i] += sV[i * P + k] * c;
       }
     }
+    for (int i = 0; i < M; ++i) io[M * M + M + i] = g[i];
   }
-  double nrm = 0;
-#pragma unroll
-  for (int i = 0; i < M; ++i) nrm = fmax(nrm, fabs(A[i][i]));
-  const double tol = M * nrm * 2.220446049250313e-16;   // MATLAB pinv: max(size(A)) * norm(A) * eps
-  double g[M];
-#pragma unroll
-  for (int i = 0; i < M; ++i) g[i] = 0;
-#pragma unroll
-  for (int k = 0; k < M; ++k) {
-    if (fabs(A[k][k]) > tol) {
-      double c = 0;
-#pragma unroll
-      for (int i = 0; i < M; ++i) c += V[i][k] * v[i];
-      c /= A[k][k];
-#pragma unroll
-      for (int i = 0; i < M; ++i) g[i] += V[i][k] * c;
-    }
-  }
-#pragma unroll
-  for (int i = 0; i < M; ++i) io[M * M + M + i] = g[i];
+  __syncwarp();
 }
 
 __global__ void k_pois_pinv(double* __restrict__ io) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) pinv_solve_1t(io);
+  __shared__ double sA[64], sV[64], cs[16];
+  if (threadIdx.x < 32) pinv_solve_warp(io, sA, sV, cs);
 }
 
 // ---------------------------------------------------------------------------- persistent AAR
@@ -250,6 +274,7 @@ __global__ void __launch_bounds__(256, 2) k_aar(const __grid_constant__ AarArgs 
   extern __shared__ double rtab[];                  // 1/r and theta scale per radial node (2 Nx)
   __shared__ double sh[32];
   __shared__ double gsh[kAarM * kAarM + 2 * kAarM];
+  __shared__ double jA[64], jV[64], jcs[16];        // Anderson solve (block 0, warp 0)
   __shared__ double C[6][kMaxFDn + 1];
   __shared__ double relres_s;
   if (threadIdx.x <= kMaxFDn) {
@@ -326,9 +351,9 @@ __global__ void __launch_bounds__(256, 2) k_aar(const __grid_constant__ AarArgs 
           gsh[k] = t;
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-          pinv_solve_1t(gsh);                        // gamma -> gsh[m*m + m ..]
-          for (int i = 0; i < m; ++i) A.gam[i] = gsh[m * m + m + i];
+        if (threadIdx.x < 32) {
+          pinv_solve_warp(gsh, jA, jV, jcs);        // gamma -> gsh[m*m + m ..]
+          if (threadIdx.x < m) A.gam[threadIdx.x] = gsh[m * m + m + threadIdx.x];
         }
       }
       if (!grid_sync(A.bar, A.status)) break;
