@@ -222,6 +222,28 @@ def max_over_ranks(value: float, dist=None) -> float:
 
 
 # ----------------------------------------------------------------------------- GPU arms
+class _NvtxRange:
+    """An NVTX range around the timed passes (so that a profiler can be limited to them with
+    ``ncu --nvtx --nvtx-include timed_scf_steps/``); a no-op when torch has no CUDA NVTX."""
+
+    def __init__(self, name):
+        self.name = name
+        self.nv = None
+
+    def __enter__(self):
+        try:
+            import torch
+            torch.cuda.nvtx.range_push(self.name)
+            self.nv = torch.cuda.nvtx
+        except Exception:
+            self.nv = None
+        return self
+
+    def __exit__(self, *a):
+        if self.nv is not None:
+            self.nv.range_pop()
+
+
 def scf_arm(S, blocks, prec, steps, warmup, ramp, e2e_steps=0, max_passes=80, scf_tol=1e-6, profile=False, clocks=None):
     """SCF of ``S`` on the GPU through cx_scf_init / cx_scf_step / cx_scf_finish.
 
@@ -249,9 +271,10 @@ def scf_arm(S, blocks, prec, steps, warmup, ramp, e2e_steps=0, max_passes=80, sc
             clocks.start()
         g.timer_start()
         timed = []
-        for _ in range(steps):
-            timed.append(g.scf_step())
-        ms = g.timer_stop()
+        with _NvtxRange("timed_scf_steps"):
+            for _ in range(steps):
+                timed.append(g.scf_step())
+            ms = g.timer_stop()
         if clocks:
             out["clocks"] = clocks.stop()
         out["ms_per_step"] = ms / max(steps, 1)

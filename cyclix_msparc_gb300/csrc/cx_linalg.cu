@@ -4,9 +4,9 @@
 //    self-adjoint in it away from the two radial end rows), the extreme Ritz values of the
 //    tridiagonal matrix found by Sturm-sequence bisection on the GPU; it stands in for
 //    eigs(Hfun,N,1,'lr'/'sr') of src/eigSolver.m:47-67 (bup = 1.01 lambda_max, a0 = lambda_min - 0.1);
-//  * Rayleigh-Ritz per block: Gram G = X^H X, M = X^H (H X) and the W-Gram X^H W X (cuBLAS;
-//    complex128, or complex64 under the BF16x9 FP32-emulation math mode: FP32-accurate tensor-core
-//    products), FP64 Cholesky G = R^H R and the pencil A = G^-1 M, whose eigenvalues are those of
+//  * Rayleigh-Ritz per block: Gram G = X^H X, M = X^H (H X) and the W-Gram X^H W X (complex128:
+//    cuBLAS ZGEMM; complex64: the tcgen05 3xTF32 kernels of cx_tcgen05.cu, FP64 sums of FP32
+//    partials), FP64 Cholesky G = R^H R and the pencil A = G^-1 M, whose eigenvalues are those of
 //    the reference's Hs = R A R^-1 (orth + psi'*H*psi of :99-104, in a basis of the same span);
 //    the eigenpairs of A (:110) through the W-similar, nearly Hermitian T = U_w A U_w^-1 and a
 //    fixed-point refinement (restarted when it stalls), the general FP64 solver as the last

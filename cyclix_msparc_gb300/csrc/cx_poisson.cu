@@ -241,22 +241,28 @@ __device__ double d_theta(const AarArgs& A, const double (*C)[kMaxFDn + 1], cons
 
 // Lap_std x at point p (matrix-free, the arithmetic of the Hamiltonian kernels' Laplacian)
 // (coefficients C: cr2, cr1, ct2, ct1, cz2, cz1 rows, staged in shared memory with 1/r and the theta scale)
-__device__ double lap_at(const AarArgs& A, const double (*C)[kMaxFDn + 1], const double* rinv, const double* thsc, const double* x,
-                         const double* vt, int p) {
+// FT > 0: the FD half-width is FT at compile time, the loop is unrolled and every neighbour load
+// is independent of the others (predicated at the walls), so a thread has them all in flight at
+// once; FT = 0: half-width A.F at run time.
+template <int FT>
+__device__ __forceinline__ double lap_at(const AarArgs& A, const double (*C)[kMaxFDn + 1], const double* rinv, const double* thsc,
+                                         const double* x, const double* vt, int p) {
   const int Nx = A.Nx, Ny = A.Ny, plane = Nx * Ny;
   const int r = p % Nx, t = (p / Nx) % Ny, z = p / plane;
+  const int F = FT > 0 ? FT : A.F;
   const double xc = ldx(x, p);
   double s2 = C[0][0] * xc, s1 = 0, st2 = C[2][0] * xc, sz = C[4][0] * xc, sx = 0;
-#pragma unroll 2
-  for (int q = 1; q <= A.F; ++q) {
+#pragma unroll
+  for (int q = 1; q <= (FT > 0 ? FT : kMaxFDn); ++q) {
+    if (FT == 0 && q > F) break;
     const double a = r + q < Nx ? ldx(x, p + q) : 0.0, b = r - q >= 0 ? ldx(x, p - q) : 0.0;
-    s2 += C[0][q] * (a + b);
-    s1 += C[1][q] * (a - b);
     const int tp = wrap_idx(t + q, Ny, A.bcy), tm = wrap_idx(t - q, Ny, A.bcy);
     const double c = tp >= 0 ? ldx(x, p + (tp - t) * Nx) : 0.0, d = tm >= 0 ? ldx(x, p + (tm - t) * Nx) : 0.0;
-    st2 += C[2][q] * (c + d);
     const int zp = wrap_idx(z + q, A.Nz, A.bcz), zm = wrap_idx(z - q, A.Nz, A.bcz);
     const double e = zp >= 0 ? ldx(x, p + (zp - z) * plane) : 0.0, g = zm >= 0 ? ldx(x, p + (zm - z) * plane) : 0.0;
+    s2 += C[0][q] * (a + b);
+    s1 += C[1][q] * (a - b);
+    st2 += C[2][q] * (c + d);
     sz += C[4][q] * (e + g);
     if (A.helical) {
       const double u = zp >= 0 ? ldx(vt, p + (zp - z) * plane) : 0.0, w = zm >= 0 ? ldx(vt, p + (zm - z) * plane) : 0.0;
@@ -270,6 +276,7 @@ __device__ double lap_at(const AarArgs& A, const double (*C)[kMaxFDn + 1], const
 // and, on a Richardson iteration, writes the next iterate x + omega res into the other buffer in
 // the same pass; one grid barrier then publishes both and the norm.  An Anderson iteration (every
 // p-th) reduces the normal equations, solves them in block 0 and updates after two more barriers.
+template <int FT>
 __global__ void __launch_bounds__(256, 2) k_aar(const __grid_constant__ AarArgs A) {
   extern __shared__ double rtab[];                  // 1/r and theta scale per radial node (2 Nx)
   __shared__ double sh[32];
@@ -308,7 +315,7 @@ __global__ void __launch_bounds__(256, 2) k_aar(const __grid_constant__ AarArgs 
     const bool anderson = count % A.p == 0;
     double s = 0;
     for (int p = tid0; p < N; p += stride) {
-      const double rv = A.f[p] - lap_at(A, C, rinv, thsc, xc, A.vt, p);
+      const double rv = A.f[p] - lap_at<FT>(A, C, rinv, thsc, xc, A.vt, p);
       const double pv = A.dinv[p] * rv;
       const double xv = xc[p];
       s += rv * rv;
@@ -347,6 +354,7 @@ __global__ void __launch_bounds__(256, 2) k_aar(const __grid_constant__ AarArgs 
       if (blockIdx.x == 0) {
         for (int k = threadIdx.x; k < m * (m + 1); k += blockDim.x) {
           double t = 0;
+#pragma unroll 8
           for (int b = 0; b < nblk; ++b) t += __ldcg(A.part + 2 * nblk + (size_t)b * m * (m + 1) + k);
           gsh[k] = t;
         }
@@ -390,14 +398,17 @@ cx_status poisson_dev(cx_handle h, const double* d_f, double* d_phi, double tol,
   if (!h || !d_f || !d_phi) return CX_ERR_ARG;
   if (maxit < 1 || !(tol > 0)) { h->err = "cx_poisson: need maxit >= 1 and tol > 0"; return CX_ERR_ARG; }
   const int N = h->g.N, m = kAarM;
-  // grid: one resident block of 256 threads per SM (cooperative launch), at most one per 256 points
+  // grid: resident blocks of 256 threads (cooperative launch)
   int dev = 0, nsm = 0, per_sm = 0;
   CX_TRY_CUDA(h, cudaGetDevice(&dev));
   CX_TRY_CUDA(h, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   const size_t dyn_smem = (size_t)2 * h->g.Nx * sizeof(double);
-  CX_TRY_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_aar, 256, dyn_smem));
+  // FD order 12 (the reference's default) has its own instance with the neighbour loop unrolled
+  const void* kern = h->g.FDn == 6 ? (const void*)k_aar<6> : (const void*)k_aar<0>;
+  CX_TRY_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, dyn_smem));
   if (per_sm < 1) { h->err = "cx_poisson: the AAR kernel does not fit on an SM"; return CX_ERR_CUDA; }
-  const int nblocks = std::max(1, std::min(nsm, (N + 255) / 256));
+  // every block resident (cooperative launch), at most one point per thread
+  const int nblocks = std::max(1, std::min(nsm * std::min(per_sm, 2), (N + 255) / 256));
   // workspace: x (two), vt, res, xold, fold, dinv (N each), DX, DF (N x m), 1/r and theta scale
   // (Nx each), per-block partials, Anderson weights, barrier word, outputs
   const size_t parts = (size_t)2 * nblocks + (size_t)nblocks * m * (m + 1);
@@ -486,7 +497,7 @@ cx_status poisson_dev(cx_handle h, const double* d_f, double* d_phi, double tol,
     A.nb = 1.0 / std::sqrt(nb2);
   }
   void* args[] = {(void*)&A};
-  CX_TRY_CUDA(h, cudaLaunchCooperativeKernel((const void*)k_aar, dim3(nblocks), dim3(256), args, dyn_smem, st));
+  CX_TRY_CUDA(h, cudaLaunchCooperativeKernel(kern, dim3(nblocks), dim3(256), args, dyn_smem, st));
   h->launches++;
   int it = 0, bst = 0;
   double rr = 0;

@@ -15,9 +15,10 @@
 //    the same work);
 //  * each plane is used once, when it arrives: its in-plane part (radial + theta + Veff) goes to
 //    the accumulator of the same output plane and its z-stencil contributions are forwarded to
-//    the accumulators of the 2 FDn planes around it.  Each thread keeps a ring of 2 FDn + 1
-//    pending output accumulators in registers; the ring is rotated by a (2 FDn + 1)-way switch
-//    over a short block of code (register indices stay compile-time, no moves, compact code);
+//    the accumulators of the 2 FDn planes around it.  Each thread keeps 2 FDn + 1 pending output
+//    accumulators in registers; slot k holds output plane z - FDn + k, and the shift to the next
+//    plane is folded into the multiply-adds (slot k <- slot k+1 + c x), so register indices stay
+//    compile-time with no moves and no branch;
 //  * helical cells: the cross term (X DG2^T) DG3^T equals D_z (D_theta X) (the two 1-D operators
 //    act on different indices and commute); D_theta of the arriving plane is formed from the
 //    same theta window and forwarded like the z-stencil terms;
@@ -110,28 +111,27 @@ __device__ __forceinline__ float2 cmulf(float2 v, float2 p) {
   return make_float2(v.x * p.x - v.y * p.y, v.x * p.y + v.y * p.x);
 }
 
-// Forward the contributions of the arriving plane z (accumulator slot U) for one row:
-//   acc[z + F] starts with cz2[F] x,  acc[z +- q] += cz2[q] x (q = 1..F),  acc[z] += in-plane part,
-//   helical: acc[z - q] += cz1[q] v, acc[z + q] -= cz1[q] v  with v = D_theta x;
-// acc[z - F] is then complete and returned.
-template <int U, bool HEL>
+// Forward the contributions of the arriving plane z for one row.  Register slot k holds the
+// pending output plane z - F + k, so moving on by one plane is a shift of the slots, folded into
+// the multiply-adds (slot k <- slot k+1 + cz2[|k - F|] x, in place in ascending k; compile-time
+// register indices, no moves and no branch):
+//   slot 2F starts with cz2[F] x,  slot F (output z) also gets the in-plane part,
+//   helical: output z - q gets + cz1[q] v and output z + q gets - cz1[q] v, with v = D_theta x;
+// slot 0 (output z - F) is then complete and returned.
+template <bool HEL>
 __device__ __forceinline__ float2 forward_row(float2 (&acc)[TM_Q], float2 x, float2 inp, float2 vth, bool is_out,
                                               const float* __restrict__ cz2, const float* __restrict__ cz1) {
   constexpr int F = TM_F, Q = TM_Q;
-  acc[(U + F) % Q] = f2mul(dup2(cz2[F]), x);
 #pragma unroll
-  for (int q = 1; q < F; ++q) acc[(U + q) % Q] = f2fma(dup2(cz2[q]), x, acc[(U + q) % Q]);
-#pragma unroll
-  for (int q = 1; q <= F; ++q) acc[(U + Q - q) % Q] = f2fma(dup2(cz2[q]), x, acc[(U + Q - q) % Q]);
-  if (is_out) acc[U] = f2add(acc[U], inp);
-  if (HEL) {
-#pragma unroll
-    for (int q = 1; q <= F; ++q) {
-      acc[(U + Q - q) % Q] = f2fma(dup2(cz1[q]), vth, acc[(U + Q - q) % Q]);
-      acc[(U + q) % Q] = f2fma(dup2(-cz1[q]), vth, acc[(U + q) % Q]);
-    }
+  for (int k = 0; k < Q - 1; ++k) {
+    const int d = k - F;                   // this slot's output plane is z + d
+    acc[k] = f2fma(dup2(cz2[d < 0 ? -d : d]), x, acc[k + 1]);
+    if (HEL && d != 0) acc[k] = f2fma(dup2(d < 0 ? cz1[-d] : -cz1[d]), vth, acc[k]);
   }
-  return acc[(U + Q - F) % Q];
+  acc[Q - 1] = f2mul(dup2(cz2[F]), x);
+  if (HEL) acc[Q - 1] = f2fma(dup2(-cz1[F]), vth, acc[Q - 1]);
+  if (is_out) acc[F] = f2add(acc[F], inp);
+  return acc[0];
 }
 
 // RPT: theta rows per thread, HEL: helical cross term
@@ -350,16 +350,8 @@ __global__ void __launch_bounds__((RPT == 1 ? TM_MAXW1 : TM_MAXW) * 32, 1) cheb_
       }
     }
     float2 done[RPT];
-#define CX_FWD(U)                                                                                 \
-  case U:                                                                                         \
-    _Pragma("unroll") for (int j = 0; j < RPT; ++j) done[j] =                                     \
-        forward_row<U, HEL>(acc[j], xv[j], inp[j], vth[j], is_out, A.cz2, A.cz1);                 \
-    break;
-    switch (it % Q) {
-      CX_FWD(0) CX_FWD(1) CX_FWD(2) CX_FWD(3) CX_FWD(4) CX_FWD(5) CX_FWD(6)
-      CX_FWD(7) CX_FWD(8) CX_FWD(9) CX_FWD(10) CX_FWD(11) CX_FWD(12)
-    }
-#undef CX_FWD
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) done[j] = forward_row<HEL>(acc[j], xv[j], inp[j], vth[j], is_out, A.cz2, A.cz1);
     if (it >= 2 * F) {                     // output plane zo = zi - F is complete
       const int zo = zi - F;
       const float2* xp_t = (const float2*)(oring + (size_t)os * A.ostage_bytes);

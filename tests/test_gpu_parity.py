@@ -2,8 +2,10 @@
 
 Tolerances (stated per test):
   * H*psi, filter: max |GPU - oracle| / max |oracle| <= 1e-12 for complex128, <= 2e-6 for complex64;
-  * subspace eigenvalues: <= 1e-9 Ha (complex128); mixed (complex64 H*X inside the Rayleigh-Ritz
-    step): <= 2.5e-4 Ha on the lowest half, <= 5e-4 Ha overall, from a random start after one filter pass;
+  * subspace eigenvalues: <= 1e-9 Ha (complex128); mixed (complex64 filter and H*X, 3xTF32
+    tensor-core Rayleigh-Ritz products): <= 3e-4 Ha on the lowest half, <= 5e-4 Ha overall, from a
+    random start after one filter pass (unconverged states; the converged mixed SCF is held to
+    1e-6 Ha in tests/test_gpu_scf.py);
   * Poisson: relative residual of the GPU potential <= the requested tolerance.
 """
 import numpy as np
@@ -126,7 +128,7 @@ def _eig_case(S, g, prec, count):
     return out
 
 
-@pytest.mark.parametrize("prec,tol,tol_low", [("fp64", 1e-9, 1e-9), ("mixed", 5e-4, 2.5e-4)])
+@pytest.mark.parametrize("prec,tol,tol_low", [("fp64", 1e-9, 1e-9), ("mixed", 5e-4, 3e-4)])
 def test_eigsolver_cyclic(small_cyclic, prec, tol, tol_low):
     from cyclix_msparc_gb300.msparc import CyclixGPU
     S = small_cyclic

@@ -7,8 +7,10 @@ Tolerances:
     occupied eigenvalues within 2e-5 Ha (both move with the 1e-6 potential tolerance), the
     per-step energies within 1e-4 Ha/atom over the common steps (the first-step spectral bounds
     come from different Krylov solvers, so trajectories differ slightly);
-  * mixed (complex64 filter, FP64 Rayleigh-Ritz, final FP64 Rayleigh-quotient refinement):
-    total energy within 1e-6 Ha/atom of the oracle.
+  * mixed (complex64 filter, 3xTF32 tensor-core Rayleigh-Ritz products with the FP64 subspace
+    eigensolver, final FP64 Rayleigh-quotient refinement): total energy within 1e-6 Ha/atom of the
+    oracle; against the GPU's own FP64 run at tight SCF tolerances, occupied eigenvalues within
+    1e-6 Ha.
 """
 import json
 from pathlib import Path
@@ -84,8 +86,9 @@ def test_scf_mixed_matches_oracle(scf_system):
 def test_scf_mixed_eigenvalues_match_fp64(case):
     """Mixed precision against plain FP64 on the GPU at a tight SCF tolerance: occupied eigenvalues
     within 1e-6 Ha and total energy within 1e-6 Ha/atom (the target's bars), after the mixed path's
-    final FP64 refinement.  Both runs converge the potential to 1e-8 so that the comparison sees
-    the arithmetic, not the SCF tolerance."""
+    final FP64 refinement.  FP64 converges the potential to 1e-8; the mixed run to 2e-7, near the
+    floor that complex64 states leave in the density (about 1e-7 relative), so that the comparison
+    sees the arithmetic rather than a loose SCF tolerance."""
     from cyclix_msparc_gb300.msparc import CyclixGPU
     name, _, nocc = CASES[case]
     wl = WORKLOADS[name]
@@ -97,11 +100,11 @@ def test_scf_mixed_eigenvalues_match_fp64(case):
         try:
             for i, (_, _, n) in enumerate(bl):
                 g.set_psi(i, initial_psi(S.N, n, 7 + i))
-            out[prec] = g.scf(S, scf_tol=1e-8, max_scf=80)
+            out[prec] = g.scf(S, scf_tol=1e-8 if prec == "fp64" else 2e-7, max_scf=80)
         finally:
             g.close()
-    (r64, ev64, *_), (r32, ev32, *_) = out["fp64"], out["mixed"]
-    assert r64.converged == 1 and r32.converged == 1
+    (r64, ev64, _, _, h64), (r32, ev32, _, _, h32) = out["fp64"], out["mixed"]
+    assert r64.converged == 1 and r32.converged == 1, (h64[-6:], h32[-6:])
     assert abs(r32.Etotal - r64.Etotal) / S.n_atm < 1e-6
     off = 0
     for (_, _, n) in bl:
