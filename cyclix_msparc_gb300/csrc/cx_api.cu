@@ -124,10 +124,16 @@ cx_status fused_step(cx_handle h, const BlockDev<R>* d_blocks, const StepScalars
                      int nstates, int in_sel, bool use_xprev, cplx<R>* cprime, bool nonlocal, double bytes, const void* maps) {
   const NonlocalDev* nlp = nullptr;
   NonlocalDev nl = h->nl;
+  const bool prof_contract = h->prof && nonlocal && nl.nseg > 0;
+  if (prof_contract) CX_TRY_CUDA(h, cudaEventRecord(h->cev, h->stream));
   if (nonlocal && nl.nseg > 0) {
     nl.node_wchi = sizeof(R) == 4 ? h->d_node_wchi32 : h->d_node_wchi64;
     nl.ent_chi = sizeof(R) == 4 ? h->d_ent_chi32 : h->d_ent_chi64;
-    CX_TRY_CUDA(h, launch_nl_contract<R>(h->g, d_blocks, d_state_tab, nstates, in_sel, nl, cprime, h->stream));
+    if (sizeof(R) == 4 && h->nltc_contract && h->use_nltc && nl.seg_phase32)
+      CX_TRY_CUDA(h, launch_nl_contract_tc(h->g, (const BlockDev<float>*)d_blocks, d_state_tab, nstates, in_sel, nl, h->nltc,
+                                           (float2*)cprime, h->d_status, h->stream));
+    else
+      CX_TRY_CUDA(h, launch_nl_contract<R>(h->g, d_blocks, d_state_tab, nstates, in_sel, nl, cprime, h->stream));
     h->launches++;
     nlp = &nl;
   }
@@ -184,8 +190,12 @@ cx_status fused_step(cx_handle h, const BlockDev<R>* d_blocks, const StepScalars
   h->launches++;
   if (h->prof) CX_TRY_CUDA(h, cudaEventRecord(h->ev1, h->stream));
   if (tma && nlp) {
-    CX_TRY_CUDA(h, launch_nl_apply<R>(h->g, d_blocks, d_scal, d_state_tab, nstates, in_sel ^ 1,
-                                      sizeof(R) == 4 ? h->chunks32 : h->chunks64, cprime, nlp->nseg, h->stream));
+    if (h->nltc_apply && h->use_nltc)
+      CX_TRY_CUDA(h, launch_nl_apply_tc(h->g, (const BlockDev<float>*)d_blocks, d_scal, d_state_tab, nstates, in_sel ^ 1, h->chunks32,
+                                        h->nltc, (const float2*)cprime, nlp->nseg, h->d_status, h->stream));
+    else
+      CX_TRY_CUDA(h, launch_nl_apply<R>(h->g, d_blocks, d_scal, d_state_tab, nstates, in_sel ^ 1,
+                                        sizeof(R) == 4 ? h->chunks32 : h->chunks64, cprime, nlp->nseg, h->stream));
     h->launches++;
   }
   if (h->prof) {
@@ -194,6 +204,11 @@ cx_status fused_step(cx_handle h, const BlockDev<R>* d_blocks, const StepScalars
     float ms = 0, ms2 = 0;
     CX_TRY_CUDA(h, cudaEventElapsedTime(&ms, h->ev0, h->ev1));
     CX_TRY_CUDA(h, cudaEventElapsedTime(&ms2, h->ev1, h->tev1));
+    if (prof_contract) {
+      float ms3 = 0;
+      CX_TRY_CUDA(h, cudaEventElapsedTime(&ms3, h->cev, h->ev0));
+      h->prof_contract_ms += ms3;
+    }
     h->prof_ms += ms;
     h->prof_apply_ms += ms2;
     h->prof_launches++;
@@ -454,6 +469,7 @@ cx_status cx_create(const cx_grid* grid, int32_t n_atm, const cx_atom* atoms, in
     return CX_ERR_CUDA;
   }
   cudaEventCreate(&h->ev0); cudaEventCreate(&h->ev1); cudaEventCreate(&h->tev0); cudaEventCreate(&h->tev1);
+  cudaEventCreate(&h->cev);
   if (cublasCreate(&h->cublas) != CUBLAS_STATUS_SUCCESS || cublasSetStream(h->cublas, h->stream) != CUBLAS_STATUS_SUCCESS) {
     g_create_err = "cx_create: cublasCreate failed";
     cx_destroy(h);
@@ -556,6 +572,19 @@ cx_status cx_create(const cx_grid* grid, int32_t n_atm, const cx_atom* atoms, in
   h->nl.atom_node_ptr = d_anp; h->nl.node_pos = d_np; h->nl.node_seg = d_ns; h->nl.atom_seg_ptr = d_asp;
   h->nl.angnum = d_an; h->nl.row_ptr = d_rp; h->nl.ent_seg = d_es; h->nl.gamma = d_g;
   h->d_node_wchi64 = d_w64; h->d_ent_chi64 = d_c64; h->d_node_wchi32 = d_w32; h->d_ent_chi32 = d_c32;
+  {
+    // tensor-core contraction operands (W Chi per atom, hi / lo tf32 in the MMA layout)
+    std::vector<int64_t> iptr;
+    std::vector<float> img;
+    if (n_atm > 0 && nl_tc_contract_images(atom_node_ptr, node_seg, atom_seg_ptr, node_wchi, iptr, img) && !img.empty()) {
+      int64_t* d_ip;
+      float* d_im;
+      if ((s = upload(h, &d_ip, iptr)) || (s = upload(h, &d_im, img))) { g_create_err = h->err; cx_destroy(h); return s; }
+      h->nltc.ct_ptr = d_ip;
+      h->nltc.ct_img = d_im;
+      h->nltc_contract = true;
+    }
+  }
   // TMA path: per-point entry start / count, float Veff and the field maps
   h->tma_ok = tma_eligible(h->g, sizeof(float2));
   if (h->tma_ok) {
@@ -599,6 +628,18 @@ cx_status cx_create(const cx_grid* grid, int32_t n_atm, const cx_atom* atoms, in
       return s;
     }
     h->chunks32 = ChunkTables{(int32_t)cp0.size(), kmax, d_cp0, d_csp, d_csg, d_ccp, d_cc32};
+    if (!cp0.empty()) {
+      // tensor-core apply operands (Chi per chunk, hi / lo tf32 in the MMA layout)
+      std::vector<int64_t> iptr;
+      std::vector<float> img;
+      nl_tc_apply_images(cseg_ptr, cchi_ptr, cchi, iptr, img);
+      int64_t* d_ip;
+      float* d_im;
+      if ((s = upload(h, &d_ip, iptr)) || (s = upload(h, &d_im, img))) { g_create_err = h->err; cx_destroy(h); return s; }
+      h->nltc.ap_ptr = d_ip;
+      h->nltc.ap_img = d_im;
+      h->nltc_apply = true;
+    }
     h->chunks64 = ChunkTables{(int32_t)cp0.size(), kmax, d_cp0, d_csp, d_csg, d_ccp, d_cc64};
     CX_TRY_CUDA(h, cudaMemset(h->d_veff32, 0, sizeof(float) * (size_t)N * nspin));
     std::vector<CUtensorMap_st> fm(nspin);
@@ -635,6 +676,7 @@ cx_status cx_destroy(cx_handle h) {
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->tev0) cudaEventDestroy(h->tev0);
   if (h->tev1) cudaEventDestroy(h->tev1);
+  if (h->cev) cudaEventDestroy(h->cev);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return CX_OK;
@@ -819,6 +861,7 @@ cx_status cx_profile_stencil(cx_handle h, int32_t enable) {
   h->prof_launches = 0;
   h->prof_ms = 0;
   h->prof_apply_ms = 0;
+  h->prof_contract_ms = 0;
   h->prof_bytes = 0;
   return CX_OK;
 }
@@ -826,6 +869,12 @@ cx_status cx_profile_stencil(cx_handle h, int32_t enable) {
 cx_status cx_profile_read_apply(cx_handle h, double* apply_ms) {
   if (!h || !apply_ms) return CX_ERR_ARG;
   *apply_ms = h->prof_apply_ms;
+  return CX_OK;
+}
+
+cx_status cx_profile_read_contract(cx_handle h, double* contract_ms) {
+  if (!h || !contract_ms) return CX_ERR_ARG;
+  *contract_ms = h->prof_contract_ms;
   return CX_OK;
 }
 

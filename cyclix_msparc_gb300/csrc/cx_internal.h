@@ -110,6 +110,27 @@ template <typename R>
 cudaError_t launch_nl_contract(const GridDev& g, const BlockDev<R>* blocks, const int2* state_tab, int nstates,
                                int in_sel, const NonlocalDev& nl, cplx<R>* cprime, cudaStream_t st);
 
+// ---------------------------------------------------------------- tensor-core projector term (cx_nl_tc.cu)
+// Device copies of the B-operand images (hi / lo tf32 parts of W Chi per atom and of Chi per
+// chunk in the tcgen05 core-matrix layout), made once per operator.
+struct NlTcImages {
+  const int64_t* ct_ptr = nullptr;   // n_atm: float offset of the atom's image
+  const float* ct_img = nullptr;
+  const int64_t* ap_ptr = nullptr;   // nchunks: float offset of the chunk's image
+  const float* ap_img = nullptr;
+};
+// host: the images (false when an atom has more than 8 images: the CUDA-core contraction is used)
+bool nl_tc_contract_images(const std::vector<int32_t>& atom_node_ptr, const std::vector<int32_t>& node_seg,
+                           const std::vector<int32_t>& atom_seg_ptr, const std::vector<double>& node_wchi, std::vector<int64_t>& ptr,
+                           std::vector<float>& img);
+void nl_tc_apply_images(const std::vector<int32_t>& cseg_ptr, const std::vector<int64_t>& cchi_ptr, const std::vector<double>& cchi,
+                        std::vector<int64_t>& ptr, std::vector<float>& img);
+cudaError_t launch_nl_contract_tc(const GridDev& g, const BlockDev<float>* blocks, const int2* state_tab, int nstates, int in_sel,
+                                  const NonlocalDev& nl, const NlTcImages& im, float2* cprime, int* status, cudaStream_t st);
+cudaError_t launch_nl_apply_tc(const GridDev& g, const BlockDev<float>* blocks, const StepScalars* scal, const int2* state_tab,
+                               int nstates, int out_sel, const ChunkTables& ct, const NlTcImages& im, const float2* cprime, int nseg,
+                               int* status, cudaStream_t st);
+
 // ---------------------------------------------------------------- TMA path (cx_stencil_tma.cu)
 // Device arrays of tensor maps used by one launch of the TMA kernel.
 struct TmaMapSet {
@@ -201,6 +222,9 @@ struct cx_handle_s {
   // TMA path (complex64): float Veff, per-point projector entry start / count, tensor maps
   float* d_veff32 = nullptr;
   cx::ChunkTables chunks32{}, chunks64{};           // projector chunks (complex64 / complex128 Chi)
+  cx::NlTcImages nltc{};                             // tensor-core projector operands (complex64)
+  bool nltc_contract = false, nltc_apply = false;    // images present: the tcgen05 kernels are used
+  bool use_nltc = true;                              // (cleared to time the CUDA-core kernels)
   void* d_fmaps = nullptr;                           // [nspin] Veff maps
   void* d_maps = nullptr;                            // block buffers: [nblk][2] X, halo and output maps
   cx::TmaMapSet tma_main{};
@@ -213,9 +237,9 @@ struct cx_handle_s {
 
   // profiling
   bool prof = false;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr, tev0 = nullptr, tev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, tev0 = nullptr, tev1 = nullptr, cev = nullptr;
   int64_t prof_launches = 0;
-  double prof_ms = 0, prof_bytes = 0, prof_apply_ms = 0;
+  double prof_ms = 0, prof_bytes = 0, prof_apply_ms = 0, prof_contract_ms = 0;
   int64_t launches = 0;
   int64_t eig_fallbacks = 0;                         // subspace eigensolves that needed the general solver
   int64_t eig_restarts = 0;                          // similarity restarts of the eigenvector refinement

@@ -8,17 +8,17 @@
 //  * every z-plane of the tile is copied HBM -> shared memory once by cp.async.bulk.tensor.4d into
 //    a ring of 1 + P stages guarded by mbarriers: the TY rows (+ FDn radial halo each side,
 //    zero-filled by TMA outside [0, Nr): the Dirichlet walls) between theta halo rows, and the
-//    plane's Veff tile (float copy).  With one theta tile the halo rows are copies of the tile's
-//    own rows times the Bloch phase, made in shared memory one plane ahead; with several tiles
-//    two more copies bring 8-row halos and the wrapping ones are multiplied by the phase in
-//    place.  Every thread reads straight theta windows (no per-element wrap logic, all warps do
-//    the same work);
+//    plane's Veff tile (float copy).  With several tiles two more copies bring 8-row halos.
+//    The theta window a warp reads is mapped onto the staged rows (with one tile, rows across the
+//    wrap are the tile's own rows mod Ny) and rows across the theta wrap are multiplied by the
+//    Bloch phase as they are loaded; the choice is uniform over the warp, and the stages are
+//    written by TMA only;
 //  * each plane is used once, when it arrives: its in-plane part (radial + theta + Veff) goes to
 //    the accumulator of the same output plane and its z-stencil contributions are forwarded to
 //    the accumulators of the 2 FDn planes around it.  Each thread keeps 2 FDn + 1 pending output
 //    accumulators in registers; slot k holds output plane z - FDn + k, and the shift to the next
 //    plane is folded into the multiply-adds (slot k <- slot k+1 + c x), so register indices stay
-//    compile-time with no moves and no branch;
+//    compile-time with no branch;
 //  * helical cells: the cross term (X DG2^T) DG3^T equals D_z (D_theta X) (the two 1-D operators
 //    act on different indices and commute); D_theta of the arriving plane is formed from the
 //    same theta window and forwarded like the z-stencil terms;
@@ -114,8 +114,9 @@ __device__ __forceinline__ float2 cmulf(float2 v, float2 p) {
 // Forward the contributions of the arriving plane z for one row.  Register slot k holds the
 // pending output plane z - F + k, so moving on by one plane is a shift of the slots, folded into
 // the multiply-adds (slot k <- slot k+1 + cz2[|k - F|] x, in place in ascending k; compile-time
-// register indices, no moves and no branch):
-//   slot 2F starts with cz2[F] x,  slot F (output z) also gets the in-plane part,
+// register indices, no branch):
+//   slot 2F starts with cz2[F] x,  slot F (output z) takes the in-plane part, which holds the
+//   centre coefficient cz2[0] with the other centre terms,
 //   helical: output z - q gets + cz1[q] v and output z + q gets - cz1[q] v, with v = D_theta x;
 // slot 0 (output z - F) is then complete and returned.
 template <bool HEL>
@@ -125,8 +126,12 @@ __device__ __forceinline__ float2 forward_row(float2 (&acc)[TM_Q], float2 x, flo
 #pragma unroll
   for (int k = 0; k < Q - 1; ++k) {
     const int d = k - F;                   // this slot's output plane is z + d
-    acc[k] = f2fma(dup2(cz2[d < 0 ? -d : d]), x, acc[k + 1]);
-    if (HEL && d != 0) acc[k] = f2fma(dup2(d < 0 ? cz1[-d] : -cz1[d]), vth, acc[k]);
+    if (d == 0) {
+      acc[k] = acc[k + 1];                 // the centre cz2[0] x is part of the in-plane term
+    } else {
+      acc[k] = f2fma(dup2(cz2[d < 0 ? -d : d]), x, acc[k + 1]);
+      if (HEL) acc[k] = f2fma(dup2(d < 0 ? cz1[-d] : -cz1[d]), vth, acc[k]);
+    }
   }
   acc[Q - 1] = f2mul(dup2(cz2[F]), x);
   if (HEL) acc[Q - 1] = f2fma(dup2(-cz1[F]), vth, acc[Q - 1]);
@@ -240,36 +245,6 @@ __global__ void __launch_bounds__((RPT == 1 ? TM_MAXW1 : TM_MAXW) * 32, 1) cheb_
     mbar_expect_tx(&ofull[s], obytes);
     tma_load_4d(dst, omap, &ofull[s], r0, t0, z0 + io, bs.y);
   };
-  // theta halo rows of the plane in stage s (one tile: phased copies of the tile's own rows;
-  // several tiles: the Bloch phase on the staged rows that wrap)
-  auto prep_halo = [&](int s) {
-    float2* P = (float2*)(ring + (size_t)s * A.stage_bytes);
-    const int nwarps = blockDim.x >> 5;
-    if (one_tile) {
-      // one warp per halo row k: rows -F..-1 (k < F) and Ny..Ny+F-1 (k >= F)
-      for (int k = wy; k < 2 * F; k += nwarps) {
-        const bool top = k < F;
-        const int dst_row = top ? H - F + k : H + Ny + (k - F);
-        const int src_row = top ? H + Ny - F + k : H + (k - F);
-        const bool ph = top ? ph_top_on : ph_bot_on;
-        const float2 p = top ? ph_tl : ph_tr;
-        for (int c = lane; c < BW; c += 32) {
-          const float2 v = P[(size_t)src_row * BW + c];
-          P[(size_t)dst_row * BW + c] = ph ? cmulf(v, p) : v;
-        }
-      }
-    } else if (fix_top || fix_bot) {
-      for (int k = wy; k < 2 * H; k += nwarps) {
-        const bool top = k < H;
-        if (top ? fix_top : fix_bot) {
-          float2* rowp = P + (size_t)(top ? k : H + TY + (k - H)) * BW;
-          const float2 p = top ? ph_tl : ph_tr;
-          for (int c = lane; c < BW; c += 32) rowp[c] = cmulf(rowp[c], p);
-        }
-      }
-    }
-  };
-
   int issued = 0, oissued = 0;
   if (threadIdx.x == 0) {
     const int n0 = min(NST, nplanes);
@@ -290,23 +265,39 @@ __global__ void __launch_bounds__((RPT == 1 ? TM_MAXW1 : TM_MAXW) * 32, 1) cheb_
 
   bool failed = false;
   int waited = 0, ocur = 0;                // planes / xprev tiles whose arrival was awaited
-  if (!mbar_wait_bounded(&full[0], 0u)) failed = true;
-  waited = 1;
-  prep_halo(0);
-  if (__syncthreads_or(failed)) failed = true;
   int s = 0, par = 0;                      // X-ring stage and parity of plane `it`
   int os = 0, opar = 0;                    // xprev-ring stage and parity
   for (int it = 0; it < nplanes && !failed; ++it) {
+    if (!mbar_wait_bounded(&full[s], (uint32_t)par)) failed = true;
+    waited = it + 1;
     const int zi = zstart + it;
     const float2* P = (const float2*)(ring + (size_t)s * A.stage_bytes);
     const float* Vt = (const float*)(ring + (size_t)s * A.stage_bytes + rows_bytes);
     const bool is_out = zi >= z0 && zi < z1;
     const bool zw = !bcz && fix_z && (zi < 0 || zi >= Nz);
     const float2 pz = zi < 0 ? ph_zl : ph_zr;
-    // theta window of this thread's rows: rows wy*RPT-F .. wy*RPT+RPT-1+F of the arriving plane
+    // theta window of this thread's rows: tile rows rho = wy*RPT-F .. wy*RPT+RPT-1+F of the
+    // arriving plane.  Rows across the theta wrap carry the Bloch phase, applied here (the choice
+    // is uniform over the warp): with one tile they are the tile's own rows rho mod Ny, with
+    // several tiles the staged halo rows, phased on the tiles at the wrap.
     float2 w[RPT + 2 * F];
 #pragma unroll
-    for (int k = 0; k < RPT + 2 * F; ++k) w[k] = P[(size_t)(H + wy * RPT - F + k) * BW + col];
+    for (int k = 0; k < RPT + 2 * F; ++k) {
+      const int rho = wy * RPT - F + k;
+      int srow = rho;
+      bool doph = false;
+      float2 ph = ph_tl;
+      if (rho < 0) {
+        if (one_tile) srow = rho + Ny;
+        doph = one_tile ? ph_top_on : fix_top;
+      } else if (rho >= TY) {
+        if (one_tile) srow = rho - Ny;
+        doph = one_tile ? ph_bot_on : fix_bot;
+        ph = ph_tr;
+      }
+      const float2 v = P[(size_t)(H + srow) * BW + col];
+      w[k] = doph ? cmulf(v, ph) : v;
+    }
     float2 xv[RPT], inp[RPT], vth[RPT];
 #pragma unroll
     for (int j = 0; j < RPT; ++j) {
@@ -372,18 +363,11 @@ __global__ void __launch_bounds__((RPT == 1 ? TM_MAXW1 : TM_MAXW) * 32, 1) cheb_
       }
       if (A.use_xprev && ++os == NOS) { os = 0; opar ^= 1; }
     }
-    // the next plane: wait for it and build its halo rows while this one is recycled
+    // every thread is done with this plane's stage: refill it
     int s1 = s + 1, par1 = par;
     if (s1 == NST) { s1 = 0; par1 ^= 1; }
-    if (it + 1 < nplanes) {
-      if (!mbar_wait_bounded(&full[s1], (uint32_t)par1)) failed = true;
-      waited = it + 2;
-      prep_halo(s1);
-    }
     if (__syncthreads_or(failed)) failed = true;
     if (!failed && threadIdx.x == 0) {
-      // halo rows were written through the generic proxy before the stage is refilled by TMA
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       if (issued < nplanes) { issue_x(issued); ++issued; }
       if (A.use_xprev && it >= 2 * F && oissued < nout) { issue_o(oissued); ++oissued; }
     }

@@ -280,6 +280,12 @@ class CyclixGPU:
         check(self.lib, self.h, self.lib.cx_profile_read_apply(self.h, C.byref(ms)))
         return ms.value
 
+    def profile_read_contract(self) -> float:
+        """Summed device time (ms) of the projector contraction launches in the profiling window."""
+        ms = C.c_double(0)
+        check(self.lib, self.h, self.lib.cx_profile_read_contract(self.h, C.byref(ms)))
+        return ms.value
+
     def eig_fallbacks(self) -> int:
         n = C.c_int64(0)
         check(self.lib, self.h, self.lib.cx_eig_fallback_count(self.h, C.byref(n)))

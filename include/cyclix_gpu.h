@@ -286,6 +286,8 @@ cx_status cx_profile_read(cx_handle h, int64_t* launches, double* total_ms, doub
 /* Device time (ms) of the separate projector-apply launches that follow the complex64 stencil
  * launches, over the same profiling window (0 for the complex128 path, which fuses it). */
 cx_status cx_profile_read_apply(cx_handle h, double* apply_ms);
+/* Summed time (ms) of the projector contraction launches since cx_profile_stencil enabled profiling. */
+cx_status cx_profile_read_contract(cx_handle h, double* contract_ms);
 /* Page-lock a caller-owned host buffer for faster copies (cudaHostRegister) and release it. */
 cx_status cx_host_register(void* ptr, size_t bytes);
 cx_status cx_host_unregister(void* ptr);
