@@ -8,11 +8,11 @@
 //  * every z-plane of the tile is copied HBM -> shared memory once by cp.async.bulk.tensor.4d into
 //    a ring of 1 + P stages guarded by mbarriers: the TY rows (+ FDn radial halo each side,
 //    zero-filled by TMA outside [0, Nr): the Dirichlet walls) between theta halo rows, and the
-//    plane's Veff tile (float copy).  With several tiles two more copies bring 8-row halos.
-//    The theta window a warp reads is mapped onto the staged rows (with one tile, rows across the
-//    wrap are the tile's own rows mod Ny) and rows across the theta wrap are multiplied by the
-//    Bloch phase as they are loaded; the choice is uniform over the warp, and the stages are
-//    written by TMA only;
+//    plane's Veff tile (float copy).  With one theta tile the halo rows are copies of the tile's
+//    own rows times the Bloch phase, made in shared memory one plane ahead; with several tiles
+//    two more copies bring 8-row halos and the wrapping ones are multiplied by the phase in
+//    place.  Every thread reads straight theta windows (no per-element wrap logic, all warps do
+//    the same work);
 //  * each plane is used once, when it arrives: its in-plane part (radial + theta + Veff) goes to
 //    the accumulator of the same output plane and its z-stencil contributions are forwarded to
 //    the accumulators of the 2 FDn planes around it.  Each thread keeps 2 FDn + 1 pending output
@@ -245,6 +245,36 @@ __global__ void __launch_bounds__((RPT == 1 ? TM_MAXW1 : TM_MAXW) * 32, 1) cheb_
     mbar_expect_tx(&ofull[s], obytes);
     tma_load_4d(dst, omap, &ofull[s], r0, t0, z0 + io, bs.y);
   };
+  // theta halo rows of the plane in stage s (one tile: phased copies of the tile's own rows;
+  // several tiles: the Bloch phase on the staged rows that wrap)
+  auto prep_halo = [&](int s) {
+    float2* P = (float2*)(ring + (size_t)s * A.stage_bytes);
+    const int nwarps = blockDim.x >> 5;
+    if (one_tile) {
+      // one warp per halo row k: rows -F..-1 (k < F) and Ny..Ny+F-1 (k >= F)
+      for (int k = wy; k < 2 * F; k += nwarps) {
+        const bool top = k < F;
+        const int dst_row = top ? H - F + k : H + Ny + (k - F);
+        const int src_row = top ? H + Ny - F + k : H + (k - F);
+        const bool ph = top ? ph_top_on : ph_bot_on;
+        const float2 p = top ? ph_tl : ph_tr;
+        for (int c = lane; c < BW; c += 32) {
+          const float2 v = P[(size_t)src_row * BW + c];
+          P[(size_t)dst_row * BW + c] = ph ? cmulf(v, p) : v;
+        }
+      }
+    } else if (fix_top || fix_bot) {
+      for (int k = wy; k < 2 * H; k += nwarps) {
+        const bool top = k < H;
+        if (top ? fix_top : fix_bot) {
+          float2* rowp = P + (size_t)(top ? k : H + TY + (k - H)) * BW;
+          const float2 p = top ? ph_tl : ph_tr;
+          for (int c = lane; c < BW; c += 32) rowp[c] = cmulf(rowp[c], p);
+        }
+      }
+    }
+  };
+
   int issued = 0, oissued = 0;
   if (threadIdx.x == 0) {
     const int n0 = min(NST, nplanes);
@@ -265,39 +295,32 @@ __global__ void __launch_bounds__((RPT == 1 ? TM_MAXW1 : TM_MAXW) * 32, 1) cheb_
 
   bool failed = false;
   int waited = 0, ocur = 0;                // planes / xprev tiles whose arrival was awaited
+  if (!mbar_wait_bounded(&full[0], 0u)) failed = true;
+  waited = 1;
+  prep_halo(0);
+  if (__syncthreads_or(failed)) failed = true;
   int s = 0, par = 0;                      // X-ring stage and parity of plane `it`
   int os = 0, opar = 0;                    // xprev-ring stage and parity
   for (int it = 0; it < nplanes && !failed; ++it) {
-    if (!mbar_wait_bounded(&full[s], (uint32_t)par)) failed = true;
-    waited = it + 1;
+    // the next plane: wait for it and build its halo rows first, so that their shared-memory
+    // round trips overlap this plane's arithmetic (nobody reads them before the barrier below)
+    int s1 = s + 1, par1 = par;
+    if (s1 == NST) { s1 = 0; par1 ^= 1; }
+    if (it + 1 < nplanes) {
+      if (!mbar_wait_bounded(&full[s1], (uint32_t)par1)) failed = true;
+      waited = it + 2;
+      prep_halo(s1);
+    }
     const int zi = zstart + it;
     const float2* P = (const float2*)(ring + (size_t)s * A.stage_bytes);
     const float* Vt = (const float*)(ring + (size_t)s * A.stage_bytes + rows_bytes);
     const bool is_out = zi >= z0 && zi < z1;
     const bool zw = !bcz && fix_z && (zi < 0 || zi >= Nz);
     const float2 pz = zi < 0 ? ph_zl : ph_zr;
-    // theta window of this thread's rows: tile rows rho = wy*RPT-F .. wy*RPT+RPT-1+F of the
-    // arriving plane.  Rows across the theta wrap carry the Bloch phase, applied here (the choice
-    // is uniform over the warp): with one tile they are the tile's own rows rho mod Ny, with
-    // several tiles the staged halo rows, phased on the tiles at the wrap.
+    // theta window of this thread's rows: rows wy*RPT-F .. wy*RPT+RPT-1+F of the arriving plane
     float2 w[RPT + 2 * F];
 #pragma unroll
-    for (int k = 0; k < RPT + 2 * F; ++k) {
-      const int rho = wy * RPT - F + k;
-      int srow = rho;
-      bool doph = false;
-      float2 ph = ph_tl;
-      if (rho < 0) {
-        if (one_tile) srow = rho + Ny;
-        doph = one_tile ? ph_top_on : fix_top;
-      } else if (rho >= TY) {
-        if (one_tile) srow = rho - Ny;
-        doph = one_tile ? ph_bot_on : fix_bot;
-        ph = ph_tr;
-      }
-      const float2 v = P[(size_t)(H + srow) * BW + col];
-      w[k] = doph ? cmulf(v, ph) : v;
-    }
+    for (int k = 0; k < RPT + 2 * F; ++k) w[k] = P[(size_t)(H + wy * RPT - F + k) * BW + col];
     float2 xv[RPT], inp[RPT], vth[RPT];
 #pragma unroll
     for (int j = 0; j < RPT; ++j) {
@@ -363,11 +386,10 @@ __global__ void __launch_bounds__((RPT == 1 ? TM_MAXW1 : TM_MAXW) * 32, 1) cheb_
       }
       if (A.use_xprev && ++os == NOS) { os = 0; opar ^= 1; }
     }
-    // every thread is done with this plane's stage: refill it
-    int s1 = s + 1, par1 = par;
-    if (s1 == NST) { s1 = 0; par1 ^= 1; }
     if (__syncthreads_or(failed)) failed = true;
     if (!failed && threadIdx.x == 0) {
+      // halo rows were written through the generic proxy before the stage is refilled by TMA
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       if (issued < nplanes) { issue_x(issued); ++issued; }
       if (A.use_xprev && it >= 2 * F && oissued < nout) { issue_o(oissued); ++oissued; }
     }
