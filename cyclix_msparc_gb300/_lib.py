@@ -20,7 +20,7 @@ PREC = {"fp64": CX_PREC_FP64, "mixed": CX_PREC_MIXED}
 EXPORTS = ["cx_create", "cx_destroy", "cx_last_error", "cx_version", "cx_set_blocks", "cx_set_veff", "cx_set_psi",
            "cx_get_psi", "cx_hpsi", "cx_chebyshev_filter", "cx_eigsolver", "cx_eigsolver_host", "cx_poisson", "cx_sync",
            "cx_timer_start", "cx_timer_stop", "cx_profile_stencil", "cx_profile_read", "cx_launch_count",
-           "cx_host_register", "cx_host_unregister", "cx_hpsi_noalloc", "cx_profile_read_apply", "cx_profile_read_contract", "cx_eig_fallback_count", "cx_scf", "cx_refine_eigenvalues", "cx_set_device",
+           "cx_host_register", "cx_host_unregister", "cx_hpsi_noalloc", "cx_profile_read_apply", "cx_profile_read_contract", "cx_set_nl_kernels", "cx_eig_fallback_count", "cx_scf", "cx_refine_eigenvalues", "cx_set_device",
            "cx_eigsolver_full", "cx_eigsolver_full_host", "cx_scf_init", "cx_scf_step", "cx_scf_finish",
            "cx_eig_hermitian_count", "cx_stencil_config"]
 
@@ -116,6 +116,7 @@ def load(build_if_missing: bool = True):
         "cx_hpsi_noalloc": ([h, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32], C.c_int32),
         "cx_profile_read_apply": ([h, dp], C.c_int32),
         "cx_profile_read_contract": ([h, dp], C.c_int32),
+        "cx_set_nl_kernels": ([h, C.c_int32], C.c_int32),
         "cx_eig_fallback_count": ([h, P(C.c_int64)], C.c_int32),
         "cx_eig_hermitian_count": ([h, P(C.c_int64)], C.c_int32),
         "cx_stencil_config": ([h, P(C.c_int32), P(C.c_int32), P(C.c_int32), C.c_char_p, C.c_int32], C.c_int32),

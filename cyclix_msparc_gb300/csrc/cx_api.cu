@@ -872,6 +872,16 @@ cx_status cx_profile_read_apply(cx_handle h, double* apply_ms) {
   return CX_OK;
 }
 
+cx_status cx_set_nl_kernels(cx_handle h, int32_t tensor_cores) {
+  if (!h) return CX_ERR_ARG;
+  if (tensor_cores && !h->nltc_contract) {
+    h->err = "cx_set_nl_kernels: the tensor-core projector kernels need at most 8 images per atom";
+    return CX_ERR_ARG;
+  }
+  h->use_nltc = tensor_cores != 0;
+  return CX_OK;
+}
+
 cx_status cx_profile_read_contract(cx_handle h, double* contract_ms) {
   if (!h || !contract_ms) return CX_ERR_ARG;
   *contract_ms = h->prof_contract_ms;

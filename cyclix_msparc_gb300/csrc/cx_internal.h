@@ -224,7 +224,7 @@ struct cx_handle_s {
   cx::ChunkTables chunks32{}, chunks64{};           // projector chunks (complex64 / complex128 Chi)
   cx::NlTcImages nltc{};                             // tensor-core projector operands (complex64)
   bool nltc_contract = false, nltc_apply = false;    // images present: the tcgen05 kernels are used
-  bool use_nltc = true;                              // (cleared to time the CUDA-core kernels)
+  bool use_nltc = false;                             // cx_set_nl_kernels: the tcgen05 projector kernels
   void* d_fmaps = nullptr;                           // [nspin] Veff maps
   void* d_maps = nullptr;                            // block buffers: [nblk][2] X, halo and output maps
   cx::TmaMapSet tma_main{};

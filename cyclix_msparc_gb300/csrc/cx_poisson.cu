@@ -155,7 +155,7 @@ struct AarArgs {
   double* fold;
   double* DX;             // N x m
   double* DF;             // N x m
-  double* part;           // per-block partial sums: [2][nblocks] ||r||^2 by iteration parity, then [nblocks][m (m + 1)]
+  double* part;           // per-block partial sums: [2][nblocks] ||r||^2 by iteration parity, then [nblocks][kNormal]
   double* gam;            // Anderson weights (m)
   unsigned* bar;          // barrier arrival word
   int* status;            // 1 when a barrier wait ran out
@@ -203,6 +203,29 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
     for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sh[k];
   return t;   // valid in thread 0
 }
+// the normal equations of the Anderson step: upper triangle of DF'DF, then DF'res
+constexpr int kNormal = kAarM * (kAarM + 1) / 2 + kAarM;
+
+// block sums of the kNormal values of every thread, written to out[0 .. kNormal) (global);
+// red: shared scratch of (blockDim.x / 32) x kNormal doubles
+__device__ __forceinline__ void block_sum_many(double (&v)[kNormal], double* red, double* out) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < kNormal; ++k) {
+    double x = v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) red[w * kNormal + k] = x;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < kNormal; k += blockDim.x) {
+    double t = 0;
+    for (int i = 0; i < nw; ++i) t += red[i * kNormal + k];
+    out[k] = t;
+  }
+  __syncthreads();
+}
+
 // sum of the n per-block partials at a (written by other blocks): every thread gets it
 __device__ __forceinline__ double sum_partials(const double* a, int n, double* sh) {
   __shared__ double tot;
@@ -282,6 +305,7 @@ __global__ void __launch_bounds__(256, 2) k_aar(const __grid_constant__ AarArgs 
   __shared__ double sh[32];
   __shared__ double gsh[kAarM * kAarM + 2 * kAarM];
   __shared__ double jA[64], jV[64], jcs[16];        // Anderson solve (block 0, warp 0)
+  __shared__ double nred[8 * kNormal];              // normal-equation block sums (8 warps)
   __shared__ double C[6][kMaxFDn + 1];
   __shared__ double relres_s;
   if (threadIdx.x <= kMaxFDn) {
@@ -331,32 +355,45 @@ __global__ void __launch_bounds__(256, 2) k_aar(const __grid_constant__ AarArgs 
     s = block_sum(s, sh);
     if (threadIdx.x == 0) A.part[(count & 1) * nblk + blockIdx.x] = s;
     if (anderson) {
-      // this block's share of the normal matrix DF'DF and DF'res (its own points, written above)
-      double* pa = A.part + 2 * nblk + (size_t)blockIdx.x * m * (m + 1);
-      for (int i = 0; i < m; ++i) {
-        double acc[kAarM + 1];
-        for (int j = 0; j <= m; ++j) acc[j] = 0;
-        for (int p = tid0; p < N; p += stride) {
-          const double di = A.DF[(size_t)i * N + p];
-          for (int j = 0; j < m; ++j) acc[j] += di * A.DF[(size_t)j * N + p];
-          acc[m] += di * A.res[p];
-        }
-        for (int j = 0; j <= m; ++j) {
-          const double t = block_sum(acc[j], sh);
-          if (threadIdx.x == 0) pa[j < m ? i * m + j : m * m + i] = t;
-        }
+      // this block's share of the normal equations over its own points (written above): the
+      // upper triangle of DF'DF and DF'res, kNormal sums reduced together
+      double acc[kNormal];
+#pragma unroll
+      for (int k = 0; k < kNormal; ++k) acc[k] = 0;
+      for (int p = tid0; p < N; p += stride) {
+        double d[kAarM];
+#pragma unroll
+        for (int j = 0; j < kAarM; ++j) d[j] = A.DF[(size_t)j * N + p];
+        const double rp = A.res[p];
+        int k = 0;
+#pragma unroll
+        for (int i = 0; i < kAarM; ++i)
+#pragma unroll
+          for (int j = i; j < kAarM; ++j) acc[k++] += d[i] * d[j];
+#pragma unroll
+        for (int i = 0; i < kAarM; ++i) acc[k++] += d[i] * rp;
       }
+      block_sum_many(acc, nred, A.part + 2 * nblk + (size_t)blockIdx.x * kNormal);
     }
     if (!grid_sync(A.bar, A.status)) break;
     relres = sqrt(sum_partials(A.part + (count & 1) * nblk, nblk, sh)) * A.nb;
     if (!(relres > A.tol)) break;   // x (= xold) is the converged iterate (aar.m:57-80)
     if (anderson) {
       if (blockIdx.x == 0) {
-        for (int k = threadIdx.x; k < m * (m + 1); k += blockDim.x) {
+        __shared__ double tot[kNormal];
+        for (int k = threadIdx.x; k < kNormal; k += blockDim.x) {
           double t = 0;
 #pragma unroll 8
-          for (int b = 0; b < nblk; ++b) t += __ldcg(A.part + 2 * nblk + (size_t)b * m * (m + 1) + k);
-          gsh[k] = t;
+          for (int b = 0; b < nblk; ++b) t += __ldcg(A.part + 2 * nblk + (size_t)b * kNormal + k);
+          tot[k] = t;
+        }
+        __syncthreads();
+        // the full symmetric matrix (row-major) and the right-hand side for the solve
+        if (threadIdx.x < m * m) {
+          const int i = threadIdx.x / m, j = threadIdx.x % m, a = min(i, j), b = max(i, j);
+          gsh[threadIdx.x] = tot[a * m - a * (a - 1) / 2 + (b - a)];
+        } else if (threadIdx.x < m * m + m) {
+          gsh[threadIdx.x] = tot[m * (m + 1) / 2 + (threadIdx.x - m * m)];
         }
         __syncthreads();
         if (threadIdx.x < 32) {

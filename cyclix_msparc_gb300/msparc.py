@@ -280,6 +280,10 @@ class CyclixGPU:
         check(self.lib, self.h, self.lib.cx_profile_read_apply(self.h, C.byref(ms)))
         return ms.value
 
+    def set_nl_kernels(self, tensor_cores: bool):
+        """Select the projector kernels of the complex64 path (cx_set_nl_kernels)."""
+        check(self.lib, self.h, self.lib.cx_set_nl_kernels(self.h, 1 if tensor_cores else 0))
+
     def profile_read_contract(self) -> float:
         """Summed device time (ms) of the projector contraction launches in the profiling window."""
         ms = C.c_double(0)

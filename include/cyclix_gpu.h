@@ -286,6 +286,11 @@ cx_status cx_profile_read(cx_handle h, int64_t* launches, double* total_ms, doub
 /* Device time (ms) of the separate projector-apply launches that follow the complex64 stencil
  * launches, over the same profiling window (0 for the complex128 path, which fuses it). */
 cx_status cx_profile_read_apply(cx_handle h, double* apply_ms);
+/* Kernels of the complex64 projector term: 0 (default) the CUDA-core contraction and apply,
+ * 1 the tcgen05 tensor-core contraction and apply (3xTF32; the apply on grids eligible for the
+ * TMA stencil).  Both compute the same term; the CUDA-core pair is the faster one on the
+ * benchmarked cells. */
+cx_status cx_set_nl_kernels(cx_handle h, int32_t tensor_cores);
 /* Summed time (ms) of the projector contraction launches since cx_profile_stencil enabled profiling. */
 cx_status cx_profile_read_contract(cx_handle h, double* contract_ms);
 /* Page-lock a caller-owned host buffer for faster copies (cudaHostRegister) and release it. */

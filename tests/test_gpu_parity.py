@@ -96,6 +96,29 @@ def test_chebyshev_filter(small_cyclic, gpu_cyclic, prec, tol):
     assert _relerr(got, ref) < tol
 
 
+@pytest.mark.parametrize("ncol", [7, 70])
+def test_tensor_core_projector_kernels(small_cyclic, small_helical, ncol):
+    """The tcgen05 projector contraction and apply (cx_set_nl_kernels(h, 1)) against the oracle:
+    complex64 H*psi and a degree-8 filter, 7 and 70 columns (one and two groups of 64 states),
+    cyclic and every helical block; same tolerances as the CUDA-core pair."""
+    from cyclix_msparc_gb300.msparc import CyclixGPU
+    for S, seed in ((small_cyclic, 31), (small_helical, 32)):
+        g = CyclixGPU(S, _blocks(S, S.extra["Ns"]), "mixed")
+        try:
+            g.set_nl_kernels(True)
+            for b, (k, spin, n) in enumerate(g.blocks):
+                H = O.Hamiltonian(S, k, S.Veff[:, spin])
+                X = _rand(S.N, ncol, seed + b)
+                assert _relerr(g.hpsi(b, X, "mixed"), H(X)) < 2e-6, (b, ncol)
+            k, spin, n = g.blocks[0]
+            H = O.Hamiltonian(S, k, S.Veff[:, spin])
+            X = _rand(S.N, min(ncol, n), seed + 7)
+            ref = O.chebyshev_filter(X, 8, 2.0, 800.0, -3.5, H)
+            assert _relerr(g.filter(0, X, 8, 2.0, 800.0, -3.5, "mixed"), ref) < 5e-6
+        finally:
+            g.close()
+
+
 def test_chebyshev_filter_helical(small_helical, gpu_helical):
     S = small_helical
     k, spin, n = gpu_helical.blocks[3]
