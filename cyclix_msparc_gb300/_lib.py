@@ -64,7 +64,8 @@ class cx_eig_params(C.Structure):
 class cx_scf_step_info(C.Structure):
     _fields_ = [("Etotal", C.c_double), ("lambda_f", C.c_double), ("err", C.c_double), ("count", C.c_int32),
                 ("n_scf", C.c_int32), ("density_updated", C.c_int32), ("converged", C.c_int32),
-                ("poisson_iters", C.c_int32), ("pad", C.c_int32), ("step_ms", C.c_double), ("poisson_ms", C.c_double)]
+                ("poisson_iters", C.c_int32), ("pad", C.c_int32), ("step_ms", C.c_double), ("poisson_ms", C.c_double),
+                ("filter_ms", C.c_double), ("rr_ms", C.c_double)]
 
 
 class cx_block(C.Structure):

@@ -470,6 +470,7 @@ cx_status cx_create(const cx_grid* grid, int32_t n_atm, const cx_atom* atoms, in
   }
   cudaEventCreate(&h->ev0); cudaEventCreate(&h->ev1); cudaEventCreate(&h->tev0); cudaEventCreate(&h->tev1);
   cudaEventCreate(&h->cev);
+  for (auto& e : h->eig_ev) cudaEventCreate(&e);
   if (cublasCreate(&h->cublas) != CUBLAS_STATUS_SUCCESS || cublasSetStream(h->cublas, h->stream) != CUBLAS_STATUS_SUCCESS) {
     g_create_err = "cx_create: cublasCreate failed";
     cx_destroy(h);
@@ -677,6 +678,8 @@ cx_status cx_destroy(cx_handle h) {
   if (h->tev0) cudaEventDestroy(h->tev0);
   if (h->tev1) cudaEventDestroy(h->tev1);
   if (h->cev) cudaEventDestroy(h->cev);
+  for (auto& e : h->eig_ev)
+    if (e) cudaEventDestroy(e);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return CX_OK;

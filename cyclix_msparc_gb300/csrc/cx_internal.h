@@ -238,6 +238,8 @@ struct cx_handle_s {
   // profiling
   bool prof = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, tev0 = nullptr, tev1 = nullptr, cev = nullptr;
+  cudaEvent_t eig_ev[3] = {nullptr, nullptr, nullptr};   // eigSolver parts (start, after filter and H X, end)
+  double last_filter_ms = 0, last_rr_ms = 0;
   int64_t prof_launches = 0;
   double prof_ms = 0, prof_bytes = 0, prof_apply_ms = 0, prof_contract_ms = 0;
   int64_t launches = 0;

@@ -1178,6 +1178,7 @@ static cx_status eigsolver_T(cx_handle h, const cx_eig_params& P, int count, dou
   const int elecgs = P.elecgs_Count < 1 ? 1 : P.elecgs_Count;
   const int rhoTrigger = elecgs > 1 ? 1 : P.rhoTrigger;
   h->restart_fail_streak = 0;
+  CX_TRY_CUDA(h, cudaEventRecord(h->eig_ev[0], h->stream));
   std::vector<int> off(nblk + 1, 0);
   for (int b = 0; b < nblk; ++b) off[b + 1] = off[b] + h->blocks[b].Ns;
   auto min_ev = [&](int b) { return *std::min_element(EigVal + off[b], EigVal + off[b + 1]); };
@@ -1232,11 +1233,19 @@ static cx_status eigsolver_T(cx_handle h, const cx_eig_params& P, int count, dou
     if ((s = check_pipeline_status(h)) != CX_OK) return s;
   }
   // ---- Rayleigh-Ritz per block
+  CX_TRY_CUDA(h, cudaEventRecord(h->eig_ev[1], h->stream));
   int nmax = 0;
   for (int b = 0; b < nblk; ++b) nmax = std::max(nmax, h->blocks[b].Ns);
   if ((s = rayleigh_ritz_all<R>(h, sel, nmax, off, EigVal)) != CX_OK) return s;
   h->psi_sel[0] = sel ^ 1;
+  CX_TRY_CUDA(h, cudaEventRecord(h->eig_ev[2], h->stream));
   CX_TRY_CUDA(h, cudaStreamSynchronize(h->stream));
+  // device time of the last call's parts: bounds + filter + H X, and the Rayleigh-Ritz steps
+  float f_ms = 0, r_ms = 0;
+  CX_TRY_CUDA(h, cudaEventElapsedTime(&f_ms, h->eig_ev[0], h->eig_ev[1]));
+  CX_TRY_CUDA(h, cudaEventElapsedTime(&r_ms, h->eig_ev[1], h->eig_ev[2]));
+  h->last_filter_ms = f_ms;
+  h->last_rr_ms = r_ms;
   return CX_OK;
 }
 

@@ -452,6 +452,8 @@ extern "C" cx_status cx_scf_step(cx_handle h, double* psi_host, double* EigVal, 
   }
   if (EigVal) std::copy(S.ev.begin(), S.ev.end(), EigVal);
   out.step_ms = ms;
+  out.filter_ms = h->last_filter_ms;
+  out.rr_ms = h->last_rr_ms;
   out.Etotal = S.Etot;
   out.lambda_f = S.lam_f;
   out.err = S.err;

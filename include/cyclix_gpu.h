@@ -259,6 +259,8 @@ typedef struct {
   double step_ms;            /* device time of the pass (CUDA events on the handle's stream; the
                                 copies of psi_host are outside it) */
   double poisson_ms;         /* device time of the Poisson solve within it */
+  double filter_ms;          /* device time of the spectral bounds, the filter and H X within it */
+  double rr_ms;              /* device time of the Rayleigh-Ritz steps of all blocks within it */
 } cx_scf_step_info;
 
 cx_status cx_scf_init(cx_handle h, const cx_scf_params* p);
