@@ -306,91 +306,6 @@ nl_contract_kernel(const int N, const int nstates, const BlockDev<R>* __restrict
   }
 }
 
-// complex64 contraction: the sums of nl_contract_kernel with packed f32x2 arithmetic (per node and
-// state: the phase product, then one FFMA2 per projector column) and a transposing butterfly
-// over the warp (31 shuffles for the warp's 32 sums, lane l ends with sum l) instead of a
-// five-level shuffle tree per sum.
-__global__ void __launch_bounds__(128)
-nl_contract_f32_kernel(const int N, const int nstates, const BlockDev<float>* __restrict__ blocks, const int2* __restrict__ state_tab,
-                       const int in_sel, const NonlocalDev nl, const float* __restrict__ node_wchi, float2* __restrict__ cprime) {
-  static_assert(NC_SPC * 2 * kAngMax == 32, "one sum per lane");
-  const int J = blockIdx.x;
-  const int gs0 = blockIdx.y * NC_SPC;
-  const int nst = min(NC_SPC, nstates - gs0);
-  const float2* y[NC_SPC];
-  const float2* ph32[NC_SPC];
-#pragma unroll
-  for (int j = 0; j < NC_SPC; ++j) {
-    const int2 bs = state_tab[gs0 + (j < nst ? j : 0)];
-    y[j] = blocks[bs.x].buf[in_sel] + (size_t)bs.y * N;
-    ph32[j] = nl.seg_phase32 + (size_t)bs.x * nl.nseg;
-  }
-  const int n0 = nl.atom_node_ptr[J], n1 = nl.atom_node_ptr[J + 1];
-  float2 a[NC_SPC][kAngMax];
-#pragma unroll
-  for (int j = 0; j < NC_SPC; ++j)
-#pragma unroll
-    for (int q = 0; q < kAngMax; ++q) a[j][q] = make_float2(0.f, 0.f);
-#pragma unroll 2
-  for (int n = n0 + threadIdx.x; n < n1; n += blockDim.x) {
-    const int pos = nl.node_pos[n];
-    const int sg = nl.node_seg[n];
-    const float4 w4 = reinterpret_cast<const float4*>(node_wchi)[n];
-    const float wq[kAngMax] = {w4.x, w4.y, w4.z, w4.w};
-#pragma unroll
-    for (int j = 0; j < NC_SPC; ++j) {
-      if (j < nst) {
-        const float2 v = y[j][pos];
-        const float2 p = ph32[j][sg];
-        // v p = (v.x p.x - v.y p.y, v.x p.y + v.y p.x)
-        const float2 vp = __ffma2_rn(make_float2(-v.y, v.y), make_float2(p.y, p.x), __fmul2_rn(make_float2(v.x, v.x), p));
-#pragma unroll
-        for (int q = 0; q < kAngMax; ++q) a[j][q] = __ffma2_rn(make_float2(wq[q], wq[q]), vp, a[j][q]);
-      }
-    }
-  }
-  // warp: transposing butterfly over the 32 sums (index j * 8 + 2 q + (im))
-  float v[32];
-#pragma unroll
-  for (int j = 0; j < NC_SPC; ++j)
-#pragma unroll
-    for (int q = 0; q < kAngMax; ++q) {
-      v[j * 8 + 2 * q] = a[j][q].x;
-      v[j * 8 + 2 * q + 1] = a[j][q].y;
-    }
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-  for (int o = 16, c = 32; o > 0; o >>= 1, c >>= 1) {
-    const bool up = (lane & o) != 0;
-#pragma unroll
-    for (int i = 0; i < c / 2; ++i) {
-      const float keep = up ? v[i + c / 2] : v[i];
-      const float send = up ? v[i] : v[i + c / 2];
-      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
-    }
-  }
-  __shared__ float red[4][32];
-  red[w][lane] = v[0];
-  __syncthreads();
-  // threads (state j, segment, q) write the scaled, re-phased coefficients: conj(p) gamma C
-  const int s0 = nl.atom_seg_ptr[J], s1 = nl.atom_seg_ptr[J + 1];
-  const int nout = nst * (s1 - s0) * kAngMax;
-  const int nw = blockDim.x >> 5;
-  for (int o = threadIdx.x; o < nout; o += blockDim.x) {
-    const int q = o % kAngMax, sg = s0 + (o / kAngMax) % (s1 - s0), j = o / (kAngMax * (s1 - s0));
-    float sx = 0, sy = 0;
-    for (int k = 0; k < nw; ++k) {
-      sx += red[k][j * 8 + 2 * q];
-      sy += red[k][j * 8 + 2 * q + 1];
-    }
-    const float gmm = (float)nl.gamma[(size_t)J * kAngMax + q];
-    sx *= gmm;
-    sy *= gmm;
-    const float2 p = nl.seg_phase32[(size_t)state_tab[gs0 + j].x * nl.nseg + sg];
-    cprime[((size_t)(gs0 + j) * nl.nseg + sg) * kAngMax + q] = make_float2(sx * p.x + sy * p.y, sy * p.x - sx * p.y);
-  }
-}
-
 // Kleinman-Bylander apply as its own pass (used after the TMA stencil, which leaves it out):
 //   out[p, s] += alpha_b * sum_{entries e of p} Chi_e . Cp[s][seg_e][:]
 // (the scatter of src/h_nonlocal_vector_mult.m:38-42, scaled like the rest of the Chebyshev step).
@@ -401,17 +316,6 @@ nl_contract_f32_kernel(const int N, const int nstates, const BlockDev<float>* __
 // coalesced Chi_c loads and broadcast shared-memory reads.
 constexpr int NA_SPW = 4;      // states per warp
 constexpr int NA_SPC = 8 * NA_SPW;
-
-// acc += x v for real x (complex64: one packed FFMA2)
-template <typename R>
-__device__ __forceinline__ void cfma_real(cplx<R>& acc, R x, cplx<R> v) {
-  acc.x = fma(x, v.x, acc.x);
-  acc.y = fma(x, v.y, acc.y);
-}
-template <>
-__device__ __forceinline__ void cfma_real<float>(float2& acc, float x, float2 v) {
-  acc = __ffma2_rn(make_float2(x, x), v, acc);
-}
 
 template <typename R>
 __global__ void __launch_bounds__(256)
@@ -445,7 +349,11 @@ nl_apply_kernel(const int N, const int Nx, const BlockDev<R>* __restrict__ block
   for (int k = 0; k < K; ++k) {
     const R x = chi[(size_t)k * 32];
 #pragma unroll
-    for (int j = 0; j < NA_SPW; ++j) cfma_real<R>(acc[j], x, cs[(sl0 + j) * K + k]);
+    for (int j = 0; j < NA_SPW; ++j) {
+      const cplx<R> v = cs[(sl0 + j) * K + k];
+      acc[j].x = fma(x, v.x, acc[j].x);
+      acc[j].y = fma(x, v.y, acc[j].y);
+    }
   }
   if (!ok) return;
 #pragma unroll
@@ -549,13 +457,6 @@ cudaError_t launch_nl_contract(const GridDev& g, const BlockDev<R>* blocks, cons
   if (nl.n_atm == 0 || nl.nseg == 0) return cudaSuccess;
   if (nstates > 65535) return cudaErrorInvalidConfiguration;
   dim3 grid((unsigned)nl.n_atm, (unsigned)((nstates + NC_SPC - 1) / NC_SPC));
-  if constexpr (sizeof(R) == 4) {
-    if (nl.seg_phase32) {
-      nl_contract_f32_kernel<<<grid, 128, 0, st>>>(g.N, nstates, (const BlockDev<float>*)blocks, state_tab, in_sel, nl,
-                                                   (const float*)nl.node_wchi, (float2*)cprime);
-      return cudaGetLastError();
-    }
-  }
   nl_contract_kernel<R><<<grid, 128, 0, st>>>(g.N, nstates, blocks, state_tab, in_sel, nl, (const R*)nl.node_wchi, cprime);
   return cudaGetLastError();
 }

@@ -249,27 +249,34 @@ __global__ void __launch_bounds__((RPT == 1 ? TM_MAXW1 : TM_MAXW) * 32, 1) cheb_
   // several tiles: the Bloch phase on the staged rows that wrap)
   auto prep_halo = [&](int s) {
     float2* P = (float2*)(ring + (size_t)s * A.stage_bytes);
-    const int nwarps = blockDim.x >> 5;
+    constexpr int BW4 = BW / 2;            // 16-byte pieces (two complex values) per staged row
     if (one_tile) {
-      // one warp per halo row k: rows -F..-1 (k < F) and Ny..Ny+F-1 (k >= F)
-      for (int k = wy; k < 2 * F; k += nwarps) {
+      // halo rows -F..-1 (k < F) and Ny..Ny+F-1 (k >= F), two complex values per thread and step
+      for (int i = threadIdx.x; i < 2 * F * BW4; i += blockDim.x) {
+        const int k = i / BW4, c = 2 * (i - k * BW4);
         const bool top = k < F;
         const int dst_row = top ? H - F + k : H + Ny + (k - F);
         const int src_row = top ? H + Ny - F + k : H + (k - F);
         const bool ph = top ? ph_top_on : ph_bot_on;
         const float2 p = top ? ph_tl : ph_tr;
-        for (int c = lane; c < BW; c += 32) {
-          const float2 v = P[(size_t)src_row * BW + c];
-          P[(size_t)dst_row * BW + c] = ph ? cmulf(v, p) : v;
+        const float4 v = *reinterpret_cast<const float4*>(P + (size_t)src_row * BW + c);
+        float4 o = v;
+        if (ph) {
+          const float2 a = cmulf(make_float2(v.x, v.y), p), b = cmulf(make_float2(v.z, v.w), p);
+          o = make_float4(a.x, a.y, b.x, b.y);
         }
+        *reinterpret_cast<float4*>(P + (size_t)dst_row * BW + c) = o;
       }
     } else if (fix_top || fix_bot) {
-      for (int k = wy; k < 2 * H; k += nwarps) {
+      for (int i = threadIdx.x; i < 2 * H * BW4; i += blockDim.x) {
+        const int k = i / BW4, c = 2 * (i - k * BW4);
         const bool top = k < H;
         if (top ? fix_top : fix_bot) {
-          float2* rowp = P + (size_t)(top ? k : H + TY + (k - H)) * BW;
+          float4* q = reinterpret_cast<float4*>(P + (size_t)(top ? k : H + TY + (k - H)) * BW + c);
           const float2 p = top ? ph_tl : ph_tr;
-          for (int c = lane; c < BW; c += 32) rowp[c] = cmulf(rowp[c], p);
+          const float4 v = *q;
+          const float2 a = cmulf(make_float2(v.x, v.y), p), b = cmulf(make_float2(v.z, v.w), p);
+          *q = make_float4(a.x, a.y, b.x, b.y);
         }
       }
     }
