@@ -445,7 +445,8 @@ def config_lines(only=None, max_scf=40, skip_steps=False):
 
 def poisson_roofline(S, recs, hbm_peak):
     """Roofline of the AAR Poisson solve (matrix-free Lap_std, Jacobi preconditioner) over the
-    passes' device time.  On GB300 the iteration is bound by the FP64 pipe, not by HBM: per point a
+    passes' device time, against GB300's FP64 rate (the solve is not HBM-bound; its vectors stay in
+    L2, and it mostly waits at grid barriers).  Per point a
     Richardson iteration does about 60 FP64 operations (the 37-point stencil with its radial and
     theta factors, the residual, the preconditioner, the history differences and the update) and
     an Anderson iteration (every p = 6th) about 50 more (the upper triangle of DF'DF and DF'res,
@@ -459,7 +460,8 @@ def poisson_roofline(S, recs, hbm_peak):
     flops = its * 60.0 * S.N + (its // 6) * 50.0 * S.N
     by = its * 4 * S.N * 8 + (its // 6) * 2 * 7 * S.N * 8
     gfs = flops / (ms * 1e-3) / 1e9
-    return {"bound": "fp64", "iters_per_step": round(its / len(recs), 1), "ms_per_step": round(ms / len(recs), 3),
+    return {"bound": "latency (grid barriers; FP64 pipe 19 % busy under ncu)", "iters_per_step": round(its / len(recs), 1),
+            "ms_per_step": round(ms / len(recs), 3),
             "achieved": round(gfs, 1), "peak": 1250.0, "peak_kind": "nominal", "unit": "GFLOP/s", "frac": round(gfs / 1250.0, 4),
             "bytes_gbs": round(by / (ms * 1e-3) / 1e9, 1), "hbm_peak_gbs": hbm_peak}
 
