@@ -24,12 +24,13 @@
 //           parts of 128 grid points of X (K-major after a register transpose), B = Cr^T, Ci^T
 //           (64 columns of C); the minus sign is the MMA's negate-B bit.
 //
-// Data movement: 4 producer warps load the operands from global memory (coalesced), split them
+// Data movement: 8 producer warps load the operands from global memory (coalesced), split them
 // into hi / lo parts and store them in the no-swizzle K-major core-matrix layout (8 rows x 16 B
 // per core matrix, 128 B apart along K, 1 KB apart along M/N); the rotation's C image is prepared
 // once in that layout and copied per stage by cp.async.bulk.  One elected thread of a fifth warp
 // issues the MMAs; stages are handed over by mbarriers (producers -> MMA: full, MMA commit ->
-// producers: empty); the accumulator is read back with tcgen05.ld by the producer warps.
+// producers: empty); the accumulator is read back with tcgen05.ld by the first 4 producer warps
+// (warp w reads tensor-memory lanes 32 w .. 32 w + 31).
 // Every wait is bounded: on a timeout the CTA records it in *status and skips to the end, where
 // its tensor memory is released.
 #include <algorithm>
@@ -41,8 +42,6 @@
 namespace cx {
 namespace tc {
 
-constexpr int kProducerWarps = 4;
-constexpr int kThreads = 32 * (kProducerWarps + 1);
 constexpr int kTileBytes = 128 * 128;   // 128 rows x 32 tf32 (K-major core matrices)
 
 // ------------------------------------------------------------------------------------ gram
@@ -51,8 +50,11 @@ constexpr int kGramXc = 64;      // X columns per tile (MMA M = 128: x^ and x~ r
 constexpr int kGramN = 128;      // Y columns per tile (MMA N)
 constexpr int kGramStageBytes = 4 * kTileBytes;   // A hi, A lo, B hi, B lo
 constexpr size_t kGramSmem = 1024 + (size_t)kGramStages * kGramStageBytes;
-constexpr int kGramPieces = (kGramXc + kGramN) * 8 / (32 * kProducerWarps);   // 16-byte pieces per producer thread and stage
-static_assert((kGramXc + kGramN) * 8 % (32 * kProducerWarps) == 0, "pieces per stage");
+// 8 producer warps (more global loads in flight per SM; the first 4 also read the accumulator back)
+constexpr int kGramProducers = 8;
+constexpr int kGramThreads = 32 * (kGramProducers + 1);
+constexpr int kGramPieces = (kGramXc + kGramN) * 8 / (32 * kGramProducers);   // 16-byte pieces per producer thread and stage
+static_assert((kGramXc + kGramN) * 8 % (32 * kGramProducers) == 0, "pieces per stage");
 
 struct GramArgs {
   const float2* X;
@@ -64,7 +66,7 @@ struct GramArgs {
   int* status;
 };
 
-__global__ void __launch_bounds__(kThreads, 1) gram_kernel(const __grid_constant__ GramArgs A) {
+__global__ void __launch_bounds__(kGramThreads, 1) gram_kernel(const __grid_constant__ GramArgs A) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full = (uint64_t*)smem;                 // [stages]
@@ -82,7 +84,7 @@ __global__ void __launch_bounds__(kThreads, 1) gram_kernel(const __grid_constant
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kGramStages; ++s) {
-      mbar_init(&full[s], 32 * kProducerWarps);
+      mbar_init(&full[s], 32 * kGramProducers);
       mbar_init(&empty[s], 1);
     }
     mbar_init(done, 1);
@@ -95,7 +97,7 @@ __global__ void __launch_bounds__(kThreads, 1) gram_kernel(const __grid_constant
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (warp < kProducerWarps) {
+  if (warp < kGramProducers) {
     // ---- producers: 64 X columns and 128 Y columns x 16 complex grid points per stage, 16 B per
     // piece, kGramPieces pieces per thread.  The next stage's pieces are loaded into registers
     // before the current ones are split and stored, so a stage's global-load latency overlaps the
@@ -105,7 +107,7 @@ __global__ void __launch_bounds__(kThreads, 1) gram_kernel(const __grid_constant
       const int kc0 = kbeg + 16 * it;
 #pragma unroll
       for (int u = 0; u < kGramPieces; ++u) {
-        const int pc = t + u * 32 * kProducerWarps;
+        const int pc = t + u * 32 * kGramProducers;
         const int col = pc >> 3, q = pc & 7;
         const int k = kc0 + 2 * q;
         const bool isx = col < kGramXc;
@@ -146,7 +148,7 @@ __global__ void __launch_bounds__(kThreads, 1) gram_kernel(const __grid_constant
       unsigned char* Blo = Bhi + kTileBytes;
 #pragma unroll
       for (int u = 0; u < kGramPieces; ++u) {
-        const int pc = t + u * 32 * kProducerWarps;
+        const int pc = t + u * 32 * kGramProducers;
         const int col = pc >> 3, q = pc & 7;
         const float4 v = cur[u];
         float4 hi, lo;
@@ -192,7 +194,7 @@ __global__ void __launch_bounds__(kThreads, 1) gram_kernel(const __grid_constant
     mma_commit(done);
   }
   // ---- epilogue: TMEM row m = 32 warp + lane -> Re (m < 64) or Im (m >= 64) of C[i0 + m % 64][j0 + .]
-  if (warp < kProducerWarps) {
+  if (warp < 4) {
     bool ok = nk > 0 && !*(volatile int*)failed;
     if (ok && !mbar_wait(done, 0)) {
       atomicExch(failed, 1);
@@ -226,6 +228,8 @@ __global__ void __launch_bounds__(kThreads, 1) gram_kernel(const __grid_constant
 
 // ------------------------------------------------------------------------------------ rotate
 constexpr int kRotStages = 2;
+constexpr int kRotProducers = 8;                  // producer warps (the first 4 also read the accumulators back)
+constexpr int kRotThreads = 32 * (kRotProducers + 1);
 constexpr int kRotM = 128;       // grid points per tile
 constexpr int kRotN = 64;        // columns of Z per tile (two accumulators: Re and Im)
 constexpr int kRotATile = kRotM * 128;   // 128 rows x 32 tf32
@@ -242,7 +246,7 @@ struct RotArgs {
   int* status;
 };
 
-__global__ void __launch_bounds__(kThreads, 1) rotate_kernel(const __grid_constant__ RotArgs A) {
+__global__ void __launch_bounds__(kRotThreads, 1) rotate_kernel(const __grid_constant__ RotArgs A) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full = (uint64_t*)smem;
@@ -258,7 +262,7 @@ __global__ void __launch_bounds__(kThreads, 1) rotate_kernel(const __grid_consta
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kRotStages; ++s) {
-      mbar_init(&full[s], 32 * kProducerWarps);
+      mbar_init(&full[s], 32 * kRotProducers);
       mbar_init(&empty[s], 1);
     }
     mbar_init(done, 1);
@@ -271,16 +275,16 @@ __global__ void __launch_bounds__(kThreads, 1) rotate_kernel(const __grid_consta
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (warp < kProducerWarps) {
+  if (warp < kRotProducers) {
     // X: 128 grid points x 32 columns per stage; a warp task = 32 points (one per lane) x 4
-    // columns, 8 tasks per warp.  The next stage's values are loaded into registers before the
+    // columns, 4 tasks per warp.  The next stage's values are loaded into registers before the
     // current ones are split and stored (the load latency overlaps the previous stage's work).
-    constexpr int kTasks = 32 / kProducerWarps;
+    constexpr int kTasks = 32 / kRotProducers;
     auto load_stage = [&](int it, float2 (&v)[kTasks][4]) {
       const int ic0 = 32 * it;
 #pragma unroll
       for (int u = 0; u < kTasks; ++u) {
-        const int task = warp + u * kProducerWarps;
+        const int task = warp + u * kRotProducers;
         const int rb = task & 3, cq = task >> 2;          // row block of 32, column quad
         const int k = k0 + 32 * rb + lane;
         const int ib = ic0 + 4 * cq;
@@ -310,7 +314,7 @@ __global__ void __launch_bounds__(kThreads, 1) rotate_kernel(const __grid_consta
       }
 #pragma unroll
       for (int u = 0; u < kTasks; ++u) {
-        const int task = warp + u * kProducerWarps;
+        const int task = warp + u * kRotProducers;
         const int rb = task & 3, cq = task >> 2;
         const int r = 32 * rb + lane;
         const float4 re = make_float4(cur[u][0].x, cur[u][1].x, cur[u][2].x, cur[u][3].x);
@@ -368,7 +372,7 @@ __global__ void __launch_bounds__(kThreads, 1) rotate_kernel(const __grid_consta
     }
     mma_commit(done);
   }
-  if (warp < kProducerWarps) {
+  if (warp < 4) {
     bool ok = nk > 0 && !*(volatile int*)failed;
     if (ok && !mbar_wait(done, 0)) {
       atomicExch(failed, 1);
@@ -454,7 +458,7 @@ cx_status tc_gram(cx_handle h, const float2* X, const float2* Y, const float* w,
   splits = (N + kchunk - 1) / kchunk;
   GramArgs a{X, Y, w, C, N, n, m, ldc, kchunk, h->d_status};
   dim3 grid((unsigned)((n + kGramXc - 1) / kGramXc), (unsigned)((m + kGramN - 1) / kGramN), (unsigned)splits);
-  gram_kernel<<<grid, kThreads, kGramSmem, h->stream>>>(a);
+  gram_kernel<<<grid, kGramThreads, kGramSmem, h->stream>>>(a);
   h->launches++;
   CX_TRY_CUDA(h, cudaGetLastError());
   return CX_OK;
@@ -476,7 +480,7 @@ cx_status tc_rotate(cx_handle h, const float2* X, const double2* C, int N, int n
   k_rot_image<<<(unsigned)std::min<size_t>((tot + 255) / 256, 152 * 16), 256, 0, h->stream>>>(C, n, m, nks, img);
   RotArgs a{X, img, Z, N, n, m, nks, h->d_status};
   dim3 grid((unsigned)((N + kRotM - 1) / kRotM), (unsigned)((m + kRotN - 1) / kRotN));
-  rotate_kernel<<<grid, kThreads, kRotSmem, h->stream>>>(a);
+  rotate_kernel<<<grid, kRotThreads, kRotSmem, h->stream>>>(a);
   h->launches += 2;
   CX_TRY_CUDA(h, cudaGetLastError());
   return CX_OK;
