@@ -247,6 +247,8 @@ struct cx_handle_s {
   int64_t eig_restarts = 0;                          // similarity restarts of the eigenvector refinement
   int64_t eig_hermitian = 0;                         // subspace eigensolves answered by the Hermitian part
   int restart_fail_streak = 0;                       // blocks in a row whose restarts ended in the general solver
+  int* rr_tier = nullptr;                            // per block: the refinement tier that succeeded last (shared by workers)
+  int rr_tier_n = 0;
   std::vector<cx_rr_worker> rr_workers;              // concurrent Rayleigh-Ritz of the blocks
 };
 

@@ -31,6 +31,10 @@ __global__ void k_f2d(const float2* __restrict__ a, double2* __restrict__ b, siz
     b[i] = make_double2((double)a[i].x, (double)a[i].y);
 }
 
+__global__ void k_r2d(const float* __restrict__ a, double* __restrict__ b, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = (double)a[i];
+}
+
 static unsigned grid_for(size_t n) { return (unsigned)std::min<size_t>((n + 255) / 256, 152 * 16); }
 
 static cx_status ensure(cx_handle h, void** p, size_t* cap, size_t bytes) {
@@ -726,7 +730,7 @@ cx_status rr_rotate<float>(cx_handle h, const float2* X, float2* out, int N, int
 // of (T + T^H)/2, whose real eigenvalues differ from the real parts of T's eigenvalues only at
 // second order in the anti-Hermitian part (its first-order term u^H T_a u is imaginary), with a
 // W-orthonormal rotation.  *path: 0 refinement, 1 general solver, 2 Hermitian part.
-static cx_status subspace_eig(cx_handle h, int n, RRWork& w, int* path) {
+static cx_status subspace_eig(cx_handle h, int n, RRWork& w, int* path, int* tier) {
   const cuDoubleComplex one = make_cuDoubleComplex(1, 0), zero = make_cuDoubleComplex(0, 0);
   const size_t n2 = (size_t)n * n;
   const unsigned gn = grid_for(n2);
@@ -743,6 +747,13 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, int* path) {
                                                 CUDA_C_64F, w.U, n, CUDA_R_64F, w.wh, CUDA_C_64F, &wsd2, &wsh2));
   wsd = std::max(wsd, wsd2);
   wsh = std::max(wsh, wsh2);
+  const bool mixed = h->prec == CX_PREC_MIXED;
+  if (mixed) {
+    CX_TRY_SOLVER(h, cusolverDnXsyevd_bufferSize(h->cusolver, h->cusolver_params, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n,
+                                                  CUDA_C_32F, w.Mf, n, CUDA_R_32F, w.Cf, CUDA_C_32F, &wsd2, &wsh2));
+    wsd = std::max(wsd, wsd2);
+    wsh = std::max(wsh, wsh2);
+  }
   cx_status s;
   if ((s = ensure(h, &h->d_ws, &h->ws_bytes, wsd + 256)) != CX_OK) return s;
   if (h->hws_bytes < wsh + 256) {
@@ -781,11 +792,25 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, int* path) {
     return CX_OK;
   };
   bool have_herm = false;     // w.U / w.wh hold the eigenpairs of (T + T^H)/2
-  auto hermitian_eig = [&]() -> cx_status {
+  bool herm_fp32 = false;     // ... computed in FP32 (the mixed path's starting point of tier 2)
+  // full: FP64 eigenpairs; otherwise, in the mixed path, FP32 ones (cheevd: GB300's FP64 rate makes
+  // the FP64 tridiagonalisation the costliest step of the Rayleigh-Ritz), which tier 2's FP64
+  // refinement of B = U^H T U then corrects
+  auto hermitian_eig = [&](bool full) -> cx_status {
     k_herm_part<<<gn, 256, 0, st>>>(w.T0, w.U, n);
     h->launches++;
-    CX_TRY_SOLVER(h, cusolverDnXsyevd(h->cusolver, h->cusolver_params, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, CUDA_C_64F,
-                                       w.U, n, CUDA_R_64F, w.wh, CUDA_C_64F, h->d_ws, h->ws_bytes, h->h_ws, h->hws_bytes, w.info));
+    herm_fp32 = mixed && !full;
+    if (herm_fp32) {
+      k_d2f<<<gn, 256, 0, st>>>(w.U, w.Mf, n2);
+      CX_TRY_SOLVER(h, cusolverDnXsyevd(h->cusolver, h->cusolver_params, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, CUDA_C_32F,
+                                         w.Mf, n, CUDA_R_32F, w.Cf, CUDA_C_32F, h->d_ws, h->ws_bytes, h->h_ws, h->hws_bytes, w.info));
+      k_f2d<<<gn, 256, 0, st>>>(w.Mf, w.U, n2);
+      k_r2d<<<(n + 255) / 256, 256, 0, st>>>((const float*)w.Cf, w.wh, n);
+      h->launches += 3;
+    } else {
+      CX_TRY_SOLVER(h, cusolverDnXsyevd(h->cusolver, h->cusolver_params, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, CUDA_C_64F,
+                                         w.U, n, CUDA_R_64F, w.wh, CUDA_C_64F, h->d_ws, h->ws_bytes, h->h_ws, h->hws_bytes, w.info));
+    }
     CX_TRY_CUDA(h, cudaMemcpyAsync(&info, w.info, sizeof(int), cudaMemcpyDeviceToHost, st));
     CX_TRY_CUDA(h, cudaStreamSynchronize(st));
     if (info != 0) {
@@ -799,7 +824,6 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, int* path) {
   // returns true when converged, with lambda in w.ev and X = I + Z in w.Z
   // The mixed path runs the first sweeps with the B Z product on the tensor cores (complex64
   // operands, FP32-accurate BF16x9 products) down to the FP32 level, then finishes in complex128.
-  const bool mixed = h->prec == CX_PREC_MIXED;
   double best_dm = 1e300;   // best step size of the last refine() call; its iterate is in w.Zbest
   auto refine = [&](bool* conv) -> cx_status {
     *conv = false;
@@ -864,11 +888,17 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, int* path) {
                                (const cuDoubleComplex*)w.Gw, n, (cuDoubleComplex*)w.T, n));
     CX_TRY_CUDA(h, cudaMemcpyAsync(w.T0, w.T, n2 * 16, cudaMemcpyDeviceToDevice, st));
     // tier 1: the filtered block is ordered like the previous Ritz vectors, so near self-consistency T
-    // itself is nearly diagonal -- refine directly (U = I)
-    CX_TRY_CUDA(h, cudaMemcpyAsync(w.B, w.T, n2 * 16, cudaMemcpyDeviceToDevice, st));
+    // itself is nearly diagonal -- refine directly (U = I).  Skipped when this block needed tier 2
+    // in its previous step (degenerate clusters keep the fixed point from converging).
     bool conv = false;
-    cx_status rs = refine(&conv);
-    if (rs != CX_OK) return rs;
+    cx_status rs = CX_OK;
+    const bool try_tier1 = *tier != 2;
+    *tier = 2;
+    if (try_tier1) {
+      CX_TRY_CUDA(h, cudaMemcpyAsync(w.B, w.T, n2 * 16, cudaMemcpyDeviceToDevice, st));
+      rs = refine(&conv);
+      if (rs != CX_OK) return rs;
+    }
     if (conv) {
       // eigenvectors of A: c = U_w^-1 X
       CX_TRY_CUDA(h, cudaMemcpyAsync(w.V, w.Z, n2 * 16, cudaMemcpyDeviceToDevice, st));
@@ -876,12 +906,15 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, int* path) {
                                  (const cuDoubleComplex*)w.Gw, n, (cuDoubleComplex*)w.V, n));
       bool ok = false;
       if ((rs = rotation_ok(&ok)) != CX_OK) return rs;
-      if (ok) return CX_OK;
+      if (ok) {
+        *tier = 1;
+        return CX_OK;
+      }
     }
     // tier 2: Hermitian eigenvectors U of (T + T^H)/2, then refine B = U^H T U (blocks of more than
     // kGeevMax states go to the Hermitian part directly: their refinement does not converge while
     // the top of the block is unconverged, and its sweeps cost O(n^3) each)
-    if ((rs = hermitian_eig()) != CX_OK) return rs;
+    if ((rs = hermitian_eig(n > kGeevMax)) != CX_OK) return rs;
     if (n > kGeevMax) goto hermitian_part;
     CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, (const cuDoubleComplex*)w.T0, n,
                                (const cuDoubleComplex*)w.U, n, &zero, (cuDoubleComplex*)w.EZ, n));
@@ -992,8 +1025,8 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, int* path) {
   // Hermitian part: eigenvalues wh (real), c = U_w^-1 U
 hermitian_part:
   *path = 2;
-  if (!have_herm) {
-    cx_status rs = hermitian_eig();
+  if (!have_herm || herm_fp32) {
+    cx_status rs = hermitian_eig(true);
     if (rs != CX_OK) return rs;
   }
   k_real_to_complex<<<(n + 255) / 256, 256, 0, st>>>(w.wh, w.ev, n);
@@ -1053,7 +1086,9 @@ static cx_status rayleigh_ritz_block(cx_handle h, int b, int sel, RRWork& w, dou
                              (const cuDoubleComplex*)w.G, n, (cuDoubleComplex*)w.Hs, n));
   // eigenpairs of Hs (general; eigSolver.m:110 -- Hs is not Hermitian for Cyclix cells)
   int path = 0;
-  if ((s = subspace_eig(h, n, w, &path)) != CX_OK) return s;
+  int tier_scratch = 0;
+  int* tier = (h->rr_tier && b < h->rr_tier_n) ? &h->rr_tier[b] : &tier_scratch;
+  if ((s = subspace_eig(h, n, w, &path, tier)) != CX_OK) return s;
   h->eig_fallbacks += path == 1 ? 1 : 0;
   h->eig_hermitian += path == 2 ? 1 : 0;
   std::vector<std::complex<double>> ev(n);
@@ -1104,6 +1139,11 @@ static cx_status make_worker(cx_handle h, cx_rr_worker& wk) {
 template <typename R>
 static cx_status rayleigh_ritz_all(cx_handle h, int sel, int nmax, const std::vector<int>& off, double* EigVal) {
   const int nblk = h->nblk;
+  if (h->rr_tier_n != nblk) {
+    delete[] h->rr_tier;
+    h->rr_tier = new int[nblk]();
+    h->rr_tier_n = nblk;
+  }
   const int nw = std::min(nblk, kRRWorkers);
   cx_status s;
   if (nw <= 1) {
@@ -1343,6 +1383,9 @@ void cx_free_extra(cx_handle h) {
   cudaFree(h->d_misc); h->d_misc = nullptr;
   cudaFree(h->d_pois); h->d_pois = nullptr;
   cudaFree(h->d_scf); h->d_scf = nullptr;
+  delete[] h->rr_tier;
+  h->rr_tier = nullptr;
+  h->rr_tier_n = 0;
 }
 
 // lambda_j = Re(sum W conj(a) b) / sum W |a|^2 for column j (one CTA per column)

@@ -30,13 +30,31 @@ __global__ void k_pois_diag(double* dinv, int Nx, int N, double xin, double dx, 
   }
 }
 
+// 1/x and 1/sqrt(x) in FP64 from an FP32 estimate and two Newton steps (23 -> 46 -> 92 correct
+// bits): a few fused multiply-adds on GB300's narrow FP64 pipe instead of the general division and
+// square-root sequences; outside the FP32 range the FP64 operations are used.
+__device__ __forceinline__ double rcp64(double x) {
+  double y = (double)__frcp_rn((float)x);
+  if (!(fabs(y) > 0.0) || !(fabs(y) < 1e37)) return 1.0 / x;
+  y = y * fma(-x, y, 2.0);
+  y = y * fma(-x, y, 2.0);
+  return y;
+}
+__device__ __forceinline__ double rsqrt64(double x) {
+  double y = (double)rsqrtf((float)x);
+  if (!(y > 0.0) || !(y < 1e37)) return 1.0 / sqrt(x);
+  y = y * fma(-0.5 * x * y, y, 1.5);
+  y = y * fma(-0.5 * x * y, y, 1.5);
+  return y;
+}
+
 // gamma = pinv(A) v for the symmetric kAarM x kAarM A in io (A row-major, then v; gamma written
 // after v), MATLAB's pinv tolerance (aar.m:74, mixing.m:104), by one warp.  Jacobi
 // eigen-decomposition A = V diag(lambda) V^T in the parallel (round-robin) ordering: the 7
 // indices plus a dummy form 4 disjoint pairs per round, 7 rounds per sweep, so the 3 real
 // rotations of a round are computed side by side and applied together as A <- J^T A J,
 // V <- V J (lane L updates entries L and L + 32 of the 8 x 8 arrays in shared memory).  A pair is
-// rotated while |a_pq| > 1e-15 sqrt(|a_pp a_qq|) (the relative criterion for positive
+// rotated while a_pq^2 > 1e-30 |a_pp a_qq| (the relative criterion for positive
 // semi-definite matrices) and set exactly to zero after its rotation; the sweeps end when a sweep
 // rotates nothing (at most 30).  Then gamma = sum over |lambda_k| > 7 max|lambda| eps of
 // V_k (V_k . v) / lambda_k.  The whole warp must call it; sA, sV are 64 doubles each, cs 4 x 4.
@@ -61,10 +79,11 @@ __device__ __noinline__ void pinv_solve_warp(double* __restrict__ io, double* __
         double c = 1.0, sn = 0.0, on = 0.0;
         if (q < M) {
           const double app = sA[p * P + p], aqq = sA[q * P + q], apq = sA[p * P + q];
-          if (fabs(apq) > 1e-300 && fabs(apq) > 1e-15 * sqrt(fabs(app * aqq))) {
-            const double th = (aqq - app) / (2 * apq);
-            const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1));
-            c = 1 / sqrt(t * t + 1);
+          if (fabs(apq) > 1e-300 && apq * apq > 1e-30 * fabs(app * aqq)) {
+            const double th = (aqq - app) * rcp64(2 * apq);
+            const double y = th * th + 1;
+            const double t = (th >= 0 ? 1.0 : -1.0) * rcp64(fabs(th) + y * rsqrt64(y));
+            c = rsqrt64(t * t + 1);
             sn = t * c;
             on = 1.0;
           }
@@ -209,14 +228,28 @@ constexpr int kNormal = kAarM * (kAarM + 1) / 2 + kAarM;
 // block sums of the kNormal values of every thread, written to out[0 .. kNormal) (global);
 // red: shared scratch of (blockDim.x / 32) x kNormal doubles
 __device__ __forceinline__ void block_sum_many(double (&v)[kNormal], double* red, double* out) {
+  static_assert(kNormal >= 32, "one transposed sum per lane");
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  // values 32 .. kNormal-1: shuffle trees (every lane ends with the warp sum)
 #pragma unroll
-  for (int k = 0; k < kNormal; ++k) {
-    double x = v[k];
+  for (int k = 32; k < kNormal; ++k) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    if (lane == 0) red[w * kNormal + k] = x;
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    if (lane == 0) red[w * kNormal + k] = v[k];
   }
+  // values 0 .. 31: a transposing butterfly (31 shuffles and adds instead of 5 per value, which
+  // matters on GB300's narrow FP64 pipe); lane l ends with the warp sum of value l
+#pragma unroll
+  for (int o = 16, c = 32; o > 0; o >>= 1, c >>= 1) {
+    const bool up = (lane & o) != 0;
+#pragma unroll
+    for (int i = 0; i < c / 2; ++i) {
+      const double keep = up ? v[i + c / 2] : v[i];
+      const double send = up ? v[i] : v[i + c / 2];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+    }
+  }
+  red[w * kNormal + lane] = v[0];
   __syncthreads();
   for (int k = threadIdx.x; k < kNormal; k += blockDim.x) {
     double t = 0;
