@@ -31,29 +31,6 @@ __global__ void k_f2d(const float2* __restrict__ a, double2* __restrict__ b, siz
     b[i] = make_double2((double)a[i].x, (double)a[i].y);
 }
 
-// ev_j = Re(u_j^H (T u_j)) / (u_j^H u_j) + 0i for the columns of U (TU = T U); one CTA per column
-__global__ void k_col_rq(const double2* __restrict__ U, const double2* __restrict__ TU, int n, double2* __restrict__ ev) {
-  const double2* u = U + (size_t)blockIdx.x * n;
-  const double2* t = TU + (size_t)blockIdx.x * n;
-  double num = 0, den = 0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    num += u[i].x * t[i].x + u[i].y * t[i].y;
-    den += u[i].x * u[i].x + u[i].y * u[i].y;
-  }
-  __shared__ double sn[32], sd[32];
-  for (int o = 16; o > 0; o >>= 1) {
-    num += __shfl_xor_sync(0xffffffffu, num, o);
-    den += __shfl_xor_sync(0xffffffffu, den, o);
-  }
-  if ((threadIdx.x & 31) == 0) { sn[threadIdx.x >> 5] = num; sd[threadIdx.x >> 5] = den; }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double a = 0, b = 0;
-    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) { a += sn[k]; b += sd[k]; }
-    ev[blockIdx.x] = make_double2(b > 0 ? a / b : 0.0, 0.0);
-  }
-}
-
 __global__ void k_r2d(const float* __restrict__ a, double* __restrict__ b, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = (double)a[i];
 }
@@ -816,10 +793,9 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, int* path, int* tie
   };
   bool have_herm = false;     // w.U / w.wh hold the eigenpairs of (T + T^H)/2
   bool herm_fp32 = false;     // ... computed in FP32 (the mixed path's starting point of tier 2)
-  // In the mixed path the eigenvectors are computed in FP32 (cheevd: at GB300's FP64 rate the FP64
-  // tridiagonalisation was the costliest step of the Rayleigh-Ritz); tier 2's FP64 refinement of
-  // B = U^H T U corrects them, and the Hermitian-part fallback takes FP64 Rayleigh quotients.
-  // full: FP64 eigenpairs in any precision.
+  // In the mixed path tier 2 starts from FP32 eigenvectors (cheevd: at GB300's FP64 rate the FP64
+  // tridiagonalisation was the costliest step of the Rayleigh-Ritz), which its FP64 refinement of
+  // B = U^H T U corrects; full: FP64 eigenpairs (the Hermitian-part result and large blocks).
   auto hermitian_eig = [&](bool full) -> cx_status {
     k_herm_part<<<gn, 256, 0, st>>>(w.T0, w.U, n);
     h->launches++;
@@ -938,7 +914,7 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, int* path, int* tie
     // tier 2: Hermitian eigenvectors U of (T + T^H)/2, then refine B = U^H T U (blocks of more than
     // kGeevMax states go to the Hermitian part directly: their refinement does not converge while
     // the top of the block is unconverged, and its sweeps cost O(n^3) each)
-    if ((rs = hermitian_eig(false)) != CX_OK) return rs;
+    if ((rs = hermitian_eig(n > kGeevMax)) != CX_OK) return rs;
     if (n > kGeevMax) goto hermitian_part;
     CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, (const cuDoubleComplex*)w.T0, n,
                                (const cuDoubleComplex*)w.U, n, &zero, (cuDoubleComplex*)w.EZ, n));
@@ -1049,19 +1025,13 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, int* path, int* tie
   // Hermitian part: eigenvalues wh (real), c = U_w^-1 U
 hermitian_part:
   *path = 2;
-  if (!have_herm) {
-    cx_status rs = hermitian_eig(false);
+  if (!have_herm || herm_fp32) {
+    // the final rotation: FP64 eigenpairs (FP32 vectors here slowed the 384-atom SCF's convergence
+    // from a 2e-6 to a 1e-5 floor)
+    cx_status rs = hermitian_eig(true);
     if (rs != CX_OK) return rs;
   }
-  if (herm_fp32) {
-    // FP32 eigenvectors: the eigenvalues as FP64 Rayleigh quotients Re(u^H T u) / u^H u (= those of
-    // the Hermitian part: u^H T_a u is imaginary), accurate to second order in the vectors' error
-    CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, (const cuDoubleComplex*)w.T0, n,
-                               (const cuDoubleComplex*)w.U, n, &zero, (cuDoubleComplex*)w.EZ, n));
-    k_col_rq<<<n, 128, 0, st>>>(w.U, w.EZ, n, w.ev);
-  } else {
-    k_real_to_complex<<<(n + 255) / 256, 256, 0, st>>>(w.wh, w.ev, n);
-  }
+  k_real_to_complex<<<(n + 255) / 256, 256, 0, st>>>(w.wh, w.ev, n);
   h->launches++;
   CX_TRY_CUDA(h, cudaMemcpyAsync(w.V, w.U, n2 * 16, cudaMemcpyDeviceToDevice, st));
   CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
