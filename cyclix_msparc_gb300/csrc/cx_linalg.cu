@@ -31,6 +31,25 @@ __global__ void k_f2d(const float2* __restrict__ a, double2* __restrict__ b, siz
     b[i] = make_double2((double)a[i].x, (double)a[i].y);
 }
 
+// ||X - I||_F^2 of an n x n complex matrix into *out (one CTA)
+__global__ void k_dist_identity2(const double2* __restrict__ X, int n, double* __restrict__ out) {
+  double t = 0;
+  const size_t n2 = (size_t)n * n;
+  for (size_t e = threadIdx.x; e < n2; e += blockDim.x) {
+    const double re = X[e].x - ((e % (size_t)(n + 1)) == 0 ? 1.0 : 0.0);
+    t += re * re + X[e].y * X[e].y;
+  }
+  __shared__ double sh[32];
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = t;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) a += sh[k];
+    *out = a;
+  }
+}
+
 __global__ void k_r2d(const float* __restrict__ a, double* __restrict__ b, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = (double)a[i];
 }
@@ -791,6 +810,18 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, int* path, int* tie
     *ok = inf == 0 && rmin > kRotMinDiag;
     return CX_OK;
   };
+  // The refined eigenvectors X = I + Z (in w.Z) of a nearly diagonal matrix: when ||Z||_F <= 1/2,
+  // the rotated block's W-Gram (I + Z)^H (I + Z) (times a unitary U in tier 2) has its smallest
+  // unit-diagonal Cholesky diagonal above 1/3 > kRotMinDiag, so the check can be skipped.
+  auto near_identity = [&](bool* yes) -> cx_status {
+    k_dist_identity2<<<1, 512, 0, st>>>(w.Z, n, w.rmin);
+    h->launches++;
+    double d2 = 1e300;
+    CX_TRY_CUDA(h, cudaMemcpyAsync(&d2, w.rmin, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CX_TRY_CUDA(h, cudaStreamSynchronize(st));
+    *yes = d2 <= 0.25;
+    return CX_OK;
+  };
   bool have_herm = false;     // w.U / w.wh hold the eigenpairs of (T + T^H)/2
   bool herm_fp32 = false;     // ... computed in FP32 (the mixed path's starting point of tier 2)
   // In the mixed path tier 2 starts from FP32 eigenvectors (cheevd: at GB300's FP64 rate the FP64
@@ -901,11 +932,12 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, int* path, int* tie
     }
     if (conv) {
       // eigenvectors of A: c = U_w^-1 X
+      bool ok = false;
+      if ((rs = near_identity(&ok)) != CX_OK) return rs;
       CX_TRY_CUDA(h, cudaMemcpyAsync(w.V, w.Z, n2 * 16, cudaMemcpyDeviceToDevice, st));
       CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n, &one,
                                  (const cuDoubleComplex*)w.Gw, n, (cuDoubleComplex*)w.V, n));
-      bool ok = false;
-      if ((rs = rotation_ok(&ok)) != CX_OK) return rs;
+      if (!ok && (rs = rotation_ok(&ok)) != CX_OK) return rs;
       if (ok) {
         *tier = 1;
         return CX_OK;
@@ -932,14 +964,15 @@ static cx_status subspace_eig(cx_handle h, int n, RRWork& w, int* path, int* tie
         if (round > 0) CX_TRY_CUDA(h, cudaMemcpyAsync(w.B, w.T, n2 * 16, cudaMemcpyDeviceToDevice, st));
         if ((rs = refine(&conv)) != CX_OK) return rs;
         if (conv) {
-          // eigenvectors of A: c = U_w^-1 (Xt X)
+          // eigenvectors of A: c = U_w^-1 (Xt X); on the first round Xt = U is unitary
+          bool ok = false;
+          if (round == 0 && (rs = near_identity(&ok)) != CX_OK) return rs;
           CX_TRY_BLAS(h, cublasZgemm(h->cublas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &one, (const cuDoubleComplex*)w.V, n,
                                      (const cuDoubleComplex*)w.Z, n, &zero, (cuDoubleComplex*)w.Hs, n));
           CX_TRY_CUDA(h, cudaMemcpyAsync(w.V, w.Hs, n2 * 16, cudaMemcpyDeviceToDevice, st));
           CX_TRY_BLAS(h, cublasZtrsm(h->cublas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n,
                                      &one, (const cuDoubleComplex*)w.Gw, n, (cuDoubleComplex*)w.V, n));
-          bool ok = false;
-          if ((rs = rotation_ok(&ok)) != CX_OK) return rs;
+          if (!ok && (rs = rotation_ok(&ok)) != CX_OK) return rs;
           if (ok) {
             h->eig_restarts += round;
             if (round > 0) h->restart_fail_streak = 0;

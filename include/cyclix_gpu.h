@@ -195,9 +195,9 @@ cx_status cx_poisson(cx_handle h, const double* f, double* phi, double tol, int3
  * X_dev, Y_dev: N x ncol column-major, complex128 (prec CX_PREC_FP64) or complex64
  * (CX_PREC_MIXED), distinct.  The projector scratch lives in a fixed 16 MiB device array of
  * the library (held by every GPU that loads it until exit); a call that needs more returns
- * CX_ERR_ARG naming the largest ncol that fits.  The first call on a device looks up that
- * array's address and should come before any stream capture.  Calls share the array: calls
- * whose work overlaps on the GPU race.  Each call waits for its own work before returning.  The call
+ * CX_ERR_ARG naming the largest ncol that fits.  Calls share the array: calls whose work
+ * overlaps on the GPU race.  Each call waits for its own work before returning (a stream
+ * synchronisation), so a call cannot be recorded into a CUDA graph.  The call
  * runs on the handle's own stream, which is not ordered after the caller's streams: X_dev must be
  * completely written (the caller synchronises the stream that wrote it) before the call. */
 cx_status cx_hpsi_noalloc(cx_handle h, int32_t blk, int32_t ncol, const void* X_dev, void* Y_dev, int32_t prec);
