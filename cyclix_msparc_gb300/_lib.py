@@ -49,7 +49,7 @@ class cx_scf_params(C.Structure):
                 ("bet", C.c_double), ("occfac", C.c_double), ("NegCharge", C.c_double), ("Eself", C.c_double),
                 ("E_corr", C.c_double), ("n_atm", C.c_int32), ("mixing_param", C.c_double),
                 ("wkpt", C.POINTER(C.c_double)), ("b", C.POINTER(C.c_double)), ("rho0", C.POINTER(C.c_double)),
-                ("refine", C.c_int32)]
+                ("refine", C.c_int32), ("fp64_tol", C.c_double)]
 
 
 class cx_scf_result(C.Structure):

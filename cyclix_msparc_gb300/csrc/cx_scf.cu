@@ -515,6 +515,24 @@ extern "C" cx_status cx_scf(cx_handle h, const cx_scf_params* P, double* EigVal,
     if ((s = cx_scf_step(h, nullptr, nullptr, nullptr)) != CX_OK) return s;
     if (S.count > 10 * (P->max_scf + S.rhoTrigger)) break;
   }
+  if (P->fp64_tol > 0 && h->prec == CX_PREC_MIXED) {
+    // FP64 finish: the same blocks in complex128 with the converted psi; the SCF state (potential,
+    // density, mixing history, bounds) carries over
+    const std::vector<cx_block> blocks = h->blocks;
+    std::vector<std::vector<double>> psi(blocks.size());
+    for (size_t b = 0; b < blocks.size(); ++b) {
+      psi[b].resize((size_t)2 * h->g.N * blocks[b].Ns);
+      if ((s = cx_get_psi(h, (int)b, psi[b].data())) != CX_OK) return s;
+    }
+    if ((s = cx_set_blocks(h, (int)blocks.size(), blocks.data(), CX_PREC_FP64)) != CX_OK) return s;
+    for (size_t b = 0; b < blocks.size(); ++b)
+      if ((s = cx_set_psi(h, (int)b, psi[b].data())) != CX_OK) return s;
+    const int start = S.count_scf;
+    while (S.err > P->fp64_tol && S.count_scf - start < P->max_scf) {
+      if ((s = cx_scf_step(h, nullptr, nullptr, nullptr)) != CX_OK) return s;
+      if (S.count > 10 * (2 * P->max_scf + S.rhoTrigger)) break;
+    }
+  }
   if (hist)
     for (size_t i = 0; i < S.hist.size() && i < 2 * (size_t)P->max_scf; ++i) hist[i] = S.hist[i];
   return cx_scf_finish(h, EigVal, rho_out, Veff_out, res);

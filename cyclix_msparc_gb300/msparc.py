@@ -187,7 +187,7 @@ class CyclixGPU:
                                                                 cptr(u) if u is not None else None, cptr(psi_packed),
                                                                 dptr(EigVal), dptr(a0), dptr(bup), dptr(lambda_cutoff)))
 
-    def _scf_params(self, S, scf_tol, poisson_tol, max_scf, min_scf, rhoTrigger, maxit_poisson, mixing_param, refine):
+    def _scf_params(self, S, scf_tol, poisson_tol, max_scf, min_scf, rhoTrigger, maxit_poisson, mixing_param, refine, fp64_tol=0.0):
         xc = S.extra.get("xc", "LDA_PW") if hasattr(S, "extra") else "LDA_PW"
         if xc != "LDA_PW":
             raise CxError(_lib.CX_ERR_ARG, f"cx_scf implements LDA_PW, not {xc}")
@@ -198,19 +198,24 @@ class CyclixGPU:
                                npl=int(S.npl), maxit_poisson=maxit_poisson, elec_T_type=int(S.elec_T_type), bet=float(S.bet),
                                occfac=float(S.occfac), NegCharge=float(S.NegCharge), Eself=float(S.Eself), E_corr=float(S.E_corr),
                                n_atm=int(S.n_atm), mixing_param=mixing_param, wkpt=dptr(wk), b=dptr(b), rho0=dptr(rho0),
-                               refine=int(self.prec == "mixed" if refine is None else refine))
+                               refine=int(self.prec == "mixed" if refine is None else refine), fp64_tol=float(fp64_tol))
         return p, (wk, b, rho0)
 
     def scf(self, S, scf_tol=1e-6, poisson_tol=-1.0, max_scf=100, min_scf=3, rhoTrigger=4, maxit_poisson=1000,
-            mixing_param=0.3, refine=None):
-        """Full SCF on the device-resident psi (cx_scf); returns (result, EigVal packed, rho, Veff, history)."""
-        p, keep = self._scf_params(S, scf_tol, poisson_tol, max_scf, min_scf, rhoTrigger, maxit_poisson, mixing_param, refine)
+            mixing_param=0.3, refine=None, fp64_tol=0.0):
+        """Full SCF on the device-resident psi (cx_scf); returns (result, EigVal packed, rho, Veff, history).
+        ``fp64_tol`` > 0 with mixed blocks: finish with FP64 passes down to that error (the blocks
+        are complex128 afterwards)."""
+        p, keep = self._scf_params(S, scf_tol, poisson_tol, max_scf, min_scf, rhoTrigger, maxit_poisson, mixing_param, refine,
+                                   fp64_tol)
         EV = np.zeros(int(sum(self.Ns)))
         rho = np.zeros(self.N)
         V = np.zeros(self.N)
         hist = np.zeros((max_scf, 2))
         res = _lib.cx_scf_result()
         check(self.lib, self.h, self.lib.cx_scf(self.h, C.byref(p), dptr(EV), dptr(rho), dptr(V), dptr(hist), C.byref(res)))
+        if fp64_tol > 0:
+            self.prec = "fp64"
         return res, EV, rho, V, hist[: res.n_scf]
 
     def scf_init(self, S, scf_tol=1e-6, poisson_tol=-1.0, max_scf=100, min_scf=3, rhoTrigger=4, maxit_poisson=1000,

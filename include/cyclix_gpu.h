@@ -222,6 +222,10 @@ typedef struct {
   const double* rho0;        /* initial density (N) */
   int32_t refine;            /* != 0: after the loop, replace the eigenvalues by FP64 Rayleigh quotients of
                                 H[Veff_in] (cx_refine_eigenvalues) and re-evaluate occupations and energy */
+  double fp64_tol;           /* > 0 with complex64 blocks (cx_scf only): after the mixed-precision loop,
+                                switch the blocks to complex128 (psi converted) and continue with FP64
+                                passes until the error is <= fp64_tol (at most max_scf more): the fixed
+                                point of the reference's arithmetic.  The blocks stay complex128. */
 } cx_scf_params;
 
 typedef struct {

@@ -113,3 +113,34 @@ def test_scf_mixed_eigenvalues_match_fp64(case):
     for (_, _, n) in bl:
         assert np.max(np.abs(ev32[off:off + nocc] - ev64[off:off + nocc])) < ev_tol
         off += n
+
+
+def test_scf_mixed_with_fp64_finish_matches_fp64():
+    """The mixed SCF finished by FP64 passes (cx_scf_params.fp64_tol) reaches the FP64 fixed point:
+    occupied eigenvalues within 1e-6 Ha and energy within 1e-6 Ha/atom of the plain FP64 SCF, both
+    converged to 1e-8 (the cyclic 12-atom cell)."""
+    from cyclix_msparc_gb300.msparc import CyclixGPU
+    name, _, nocc = CASES[0]
+    wl = WORKLOADS[name]
+    S = make_system(wl)
+    bl = block_layout(wl, S)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        g = CyclixGPU(S, bl, prec)
+        try:
+            for i, (_, _, n) in enumerate(bl):
+                g.set_psi(i, initial_psi(S.N, n, 7 + i))
+            if prec == "fp64":
+                out[prec] = g.scf(S, scf_tol=1e-8, max_scf=80)
+            else:
+                out[prec] = g.scf(S, scf_tol=2e-7, max_scf=80, fp64_tol=1e-8)
+        finally:
+            g.close()
+    (r64, ev64, _, _, h64), (r32, ev32, _, _, h32) = out["fp64"], out["mixed"]
+    assert r64.converged == 1 and r32.converged == 1, (h64[-4:], h32[-4:])
+    assert r32.err <= 1e-8
+    assert abs(r32.Etotal - r64.Etotal) / S.n_atm < 1e-6
+    off = 0
+    for (_, _, n) in bl:
+        assert np.max(np.abs(ev32[off:off + nocc] - ev64[off:off + nocc])) < 1e-6
+        off += n
