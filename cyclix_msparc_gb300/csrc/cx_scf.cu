@@ -527,13 +527,17 @@ extern "C" cx_status cx_scf(cx_handle h, const cx_scf_params* P, double* EigVal,
     if ((s = cx_set_blocks(h, (int)blocks.size(), blocks.data(), CX_PREC_FP64)) != CX_OK) return s;
     for (size_t b = 0; b < blocks.size(); ++b)
       if ((s = cx_set_psi(h, (int)b, psi[b].data())) != CX_OK) return s;
+    // the passes mix until the FP64 tolerance is met (the step mixes while err > its scf_tol)
+    S.P.scf_tol = P->fp64_tol;
     const int start = S.count_scf;
     while (S.err > P->fp64_tol && S.count_scf - start < P->max_scf) {
       if ((s = cx_scf_step(h, nullptr, nullptr, nullptr)) != CX_OK) return s;
       if (S.count > 10 * (2 * P->max_scf + S.rhoTrigger)) break;
     }
   }
-  if (hist)
-    for (size_t i = 0; i < S.hist.size() && i < 2 * (size_t)P->max_scf; ++i) hist[i] = S.hist[i];
+  if (hist) {
+    const size_t cap = (P->fp64_tol > 0 ? 4 : 2) * (size_t)P->max_scf;   // rows: max_scf, or 2 max_scf with the FP64 finish
+    for (size_t i = 0; i < S.hist.size() && i < cap; ++i) hist[i] = S.hist[i];
+  }
   return cx_scf_finish(h, EigVal, rho_out, Veff_out, res);
 }

@@ -211,7 +211,7 @@ class CyclixGPU:
         EV = np.zeros(int(sum(self.Ns)))
         rho = np.zeros(self.N)
         V = np.zeros(self.N)
-        hist = np.zeros((max_scf, 2))
+        hist = np.zeros((2 * max_scf if fp64_tol > 0 else max_scf, 2))
         res = _lib.cx_scf_result()
         check(self.lib, self.h, self.lib.cx_scf(self.h, C.byref(p), dptr(EV), dptr(rho), dptr(V), dptr(hist), C.byref(res)))
         if fp64_tol > 0:

@@ -239,8 +239,8 @@ typedef struct {
 /* S = scf(S) (src/scf.m:1-327) on the device-resident psi of the handle's blocks: initial
  * potential from rho0, then eigSolver / occupations / density / Poisson / LDA_PW / energy /
  * Periodic-Pulay potential mixing until converged.  EigVal (packed, sum Ns), rho (N), Veff (N)
- * and hist (max_scf x 2: energy per atom, error per SCF step) are outputs (rho, Veff, hist may
- * be NULL). */
+ * and hist (max_scf x 2, or 2 max_scf x 2 with p->fp64_tol > 0: energy per atom, error per SCF
+ * step) are outputs (rho, Veff, hist may be NULL). */
 cx_status cx_scf(cx_handle h, const cx_scf_params* p, double* EigVal, double* rho, double* Veff, double* hist,
                  cx_scf_result* res);
 
