@@ -143,8 +143,8 @@ cx_status fused_step(cx_handle h, const BlockDev<R>* d_blocks, const StepScalars
     // state set times every (rows per thread, prefetch depth) configuration twice and keeps the
     // fastest for this handle; every configuration computes the same values
     if (tma && !h->tma_tuned && !use_xprev && nstates >= 64) {
-      int rp[16], dp[16];
-      const int nc = tma_candidates(h->g, rp, dp, 16);
+      int rp[24], dp[24];
+      const int nc = tma_candidates(h->g, rp, dp, 24);
       cudaEvent_t e0, e1;
       CX_TRY_CUDA(h, cudaEventCreate(&e0));
       CX_TRY_CUDA(h, cudaEventCreate(&e1));

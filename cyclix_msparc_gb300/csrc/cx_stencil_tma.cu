@@ -473,11 +473,14 @@ static bool tile_geometry(const GridDev& g, TileGeom* t, int rpt = 0, int p_req 
 
 // (rows per thread, prefetch depth) candidates of the autotuner for this grid
 int tma_candidates(const GridDev& g, int* rpt, int* depth, int cap) {
+  // ring depths 2..6 and 8 (odd ones too: at 3 rows per thread a depth of 5 still keeps two CTAs
+  // per SM, 6 does not)
+  static const int depths[] = {2, 3, 4, 5, 6, 8};
   int n = 0;
   for (int r = 1; r <= 3; ++r)
-    for (int p = 2; p <= TM_PMAX; p += 2) {
+    for (int p : depths) {
       TileGeom t;
-      if (n < cap && tile_geometry(g, &t, r, p)) { rpt[n] = r; depth[n] = p; ++n; }
+      if (p <= TM_PMAX && n < cap && tile_geometry(g, &t, r, p)) { rpt[n] = r; depth[n] = p; ++n; }
     }
   return n;
 }
