@@ -54,8 +54,9 @@ enum {
 /* Arithmetic of the filter / subspace path. */
 enum {
   CX_PREC_FP64 = 0,      /* complex128 everywhere: the plain FP64 path */
-  CX_PREC_MIXED = 1      /* complex64 filter and H*psi, 3xBF16 tensor-core subspace GEMMs with FP32
-                            accumulation, FP64 Cholesky / eigensolver / refinement */
+  CX_PREC_MIXED = 1      /* complex64 filter and H*psi, tcgen05 3xTF32 Rayleigh-Ritz products (FP32
+                            accumulation over short ranges, FP64 across them), FP64 Cholesky /
+                            eigensolver / refinement */
 };
 
 typedef struct cx_handle_s* cx_handle;
