@@ -16,13 +16,15 @@ LIB_PATH = HERE / "libcyclix_gpu.so"
 CX_OK, CX_ERR_ARG, CX_ERR_CUDA, CX_ERR_NOMEM, CX_ERR_LIB, CX_ERR_NOTPD, CX_ERR_STATE, CX_ERR_NOCONV = range(8)
 CX_PREC_FP64, CX_PREC_MIXED = 0, 1
 PREC = {"fp64": CX_PREC_FP64, "mixed": CX_PREC_MIXED}
+CX_XC_LDA_PW, CX_XC_LDA_PZ, CX_XC_GGA_PBE = 0, 1, 2
+XC = {"LDA_PW": CX_XC_LDA_PW, "LDA_PZ": CX_XC_LDA_PZ, "GGA_PBE": CX_XC_GGA_PBE}
 
 EXPORTS = ["cx_create", "cx_destroy", "cx_last_error", "cx_version", "cx_set_blocks", "cx_set_veff", "cx_set_psi",
            "cx_get_psi", "cx_hpsi", "cx_chebyshev_filter", "cx_eigsolver", "cx_eigsolver_host", "cx_poisson", "cx_sync",
            "cx_timer_start", "cx_timer_stop", "cx_profile_stencil", "cx_profile_read", "cx_launch_count",
            "cx_host_register", "cx_host_unregister", "cx_hpsi_noalloc", "cx_profile_read_apply", "cx_profile_read_contract", "cx_set_nl_kernels", "cx_eig_fallback_count", "cx_scf", "cx_refine_eigenvalues", "cx_set_device",
            "cx_eigsolver_full", "cx_eigsolver_full_host", "cx_scf_init", "cx_scf_step", "cx_scf_finish",
-           "cx_eig_hermitian_count", "cx_stencil_config"]
+           "cx_eig_hermitian_count", "cx_stencil_config", "cx_xc"]
 
 
 class cx_grid(C.Structure):
@@ -49,7 +51,7 @@ class cx_scf_params(C.Structure):
                 ("bet", C.c_double), ("occfac", C.c_double), ("NegCharge", C.c_double), ("Eself", C.c_double),
                 ("E_corr", C.c_double), ("n_atm", C.c_int32), ("mixing_param", C.c_double),
                 ("wkpt", C.POINTER(C.c_double)), ("b", C.POINTER(C.c_double)), ("rho0", C.POINTER(C.c_double)),
-                ("refine", C.c_int32), ("fp64_tol", C.c_double)]
+                ("refine", C.c_int32), ("fp64_tol", C.c_double), ("xc", C.c_int32)]
 
 
 class cx_scf_result(C.Structure):
@@ -127,6 +129,7 @@ def load(build_if_missing: bool = True):
         "cx_scf_step": ([h, dp, dp, P(cx_scf_step_info)], C.c_int32),
         "cx_scf_finish": ([h, dp, dp, dp, P(cx_scf_result)], C.c_int32),
         "cx_set_device": ([C.c_int32], C.c_int32),
+        "cx_xc": ([h, C.c_int32, dp, dp, dp], C.c_int32),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

@@ -460,6 +460,7 @@ cx_status cx_create(const cx_grid* grid, int32_t n_atm, const cx_atom* atoms, in
     h->coef.ct1[q] = q == 0 ? 0.0 : -2.0 * G.twist * G.w1[q] / G.dy;
     h->coef.cz2[q] = G.w2[q] / (G.dz * G.dz);
     h->coef.cz1[q] = q == 0 ? 0.0 : G.w1[q] / G.dz;
+    h->w1[q] = G.w1[q];
   }
   h->W.assign(G.W, G.W + N);
   cudaError_t e;

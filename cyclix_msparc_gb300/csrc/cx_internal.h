@@ -173,6 +173,7 @@ struct cx_handle_s {
   cx_grid grid{};
   cx::GridDev g{};
   cx::StencilCoef coef{};
+  double w1[cx::kMaxFDn + 1] = {};   // S.w1, first-derivative weights (gradients of the GGA potential)
   std::vector<double> W;      // host copy
   double* d_W = nullptr;
   float* d_W32 = nullptr;                            // float copy of W for the complex64 kernels

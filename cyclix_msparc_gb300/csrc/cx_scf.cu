@@ -2,7 +2,8 @@
 // potential mixing -- the reference defaults of src/initialization.m:1004-1040):
 //   Veff0 = phi[rho0] + Vxc[rho0];  loop: eigSolver step; occupations (Fermi level of
 //   src/occupations.m); from count >= rhoTrigger: density (src/electronDensity.m:9-12), Poisson
-//   (src/poissonSolve.m), LDA_PW Vxc (src/exchangeCorrelationPotential.m:82-106), total energy
+//   (src/poissonSolve.m), Vxc of S.xc: LDA_PW (src/exchangeCorrelationPotential.m:82-106), LDA_PZ
+//   or GGA_PBE (:156-362, on the FD gradients of the Cyclix grid), total energy
 //   (src/evaluateTotalEnergy.m:12-93) with the Escc correction (src/scf.m:152), error
 //   ||Veff - Veff_in|| / ||Veff|| (src/scf.m:177) and Periodic-Pulay mixing (src/mixing.m:20-116).
 // All N-length arithmetic is FP64 on the device; the host only drives the loop and reads scalars.
@@ -11,10 +12,12 @@
 #include <vector>
 
 #include "cx_common.h"
+#include "cx_xc_point.h"
 
 namespace cx {
 
-constexpr double kXcRhoTol = 1e-14;   // src/initialization.m:143
+constexpr double kXcRhoTol = xc::kRhoTol;   // src/initialization.m:143
+static_assert(xc::kGradMaxFDn == kMaxFDn, "gradient stencils cover every supported FD order");
 constexpr int kMixHist = 7;           // src/initialization.m:1035
 
 // Fermi level by bisection on sum_b occfac w_b sum_i occ(lambda_i) + NegCharge = 0, then the
@@ -102,28 +105,37 @@ __global__ void k_poisson_rhs(const double* __restrict__ rho, const double* __re
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) f[p] = -4.0 * M_PI * (rho[p] + b[p]);
 }
 
+// block partial sums of kNSums values: one per block in partial[block * kNSums + k]
+constexpr int kNSums = 7;
+__device__ __forceinline__ void block_partials(const double (&s)[kNSums], double* __restrict__ partial) {
+  __shared__ double red[kNSums][32];
+#pragma unroll
+  for (int k = 0; k < kNSums; ++k) {
+    double v = s[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < kNSums) {
+    double t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[threadIdx.x][w];
+    partial[(size_t)blockIdx.x * kNSums + threadIdx.x] = t;
+  }
+}
+
 // LDA_PW exchange-correlation (src/exchangeCorrelationPotential.m:82-106 for Vxc,
 // src/evaluateTotalEnergy.m:28-43 for the energy density), Veff = phi + Vxc, and the block
 // partial sums of: [0] ec rho_c W, [1] rho_c^(4/3) W, [2] Vxc rho_c W, [3] (b - rho) phi W,
 // [4] (Veff - Veff_in) rho W, [5] (Veff - Veff_in)^2, [6] Veff^2.
-constexpr int kNSums = 7;
 __global__ void k_xc_veff(const double* __restrict__ rho, const double* __restrict__ phi, const double* __restrict__ b,
                           const double* __restrict__ W, const double* __restrict__ veff_in, double* __restrict__ vxc,
                           double* __restrict__ veff, int N, double* __restrict__ partial) {
-  const double A = 0.031091, alpha1 = 0.21370, beta1 = 7.5957, beta2 = 3.5876, beta3 = 1.6382, beta4 = 0.49294;
-  const double C3 = 0.9847450218427;
   double s[kNSums] = {0, 0, 0, 0, 0, 0, 0};
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) {
     const double r0 = rho[p];
     const double rc = r0 < kXcRhoTol ? kXcRhoTol : r0;
-    const double rs = cbrt(0.75 / (M_PI * rc));
-    const double srs = sqrt(rs);
-    const double Q = 2 * A * (beta1 * srs + beta2 * rs + beta3 * rs * srs + beta4 * rs * rs);
-    const double lg = log(1 + 1 / Q);
-    const double dQ = A * (beta1 / srs + 2 * beta2 + 3 * beta3 * srs + 4 * beta4 * rs);
-    const double v = -C3 * cbrt(rc) + (-2 * A * (1 + alpha1 * rs)) * lg -
-                     (rs / 3) * (-2 * A * alpha1 * lg - ((-2 * A * (1 + alpha1 * rs)) * dQ) / (Q * Q + Q));
-    const double ec = -2 * A * (1 + alpha1 * rs) * lg;
+    double v, ec;
+    xc::lda_pw(rc, v, ec);
     vxc[p] = v;
     const double ve = phi[p] + v;
     veff[p] = ve;
@@ -137,18 +149,69 @@ __global__ void k_xc_veff(const double* __restrict__ rho, const double* __restri
     s[5] += d * d;
     s[6] += ve * ve;
   }
-  __shared__ double red[kNSums][32];
-#pragma unroll
-  for (int k = 0; k < kNSums; ++k) {
-    double v = s[k];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = v;
+  block_partials(s, partial);
+}
+
+// Veff = phi + Vxc for a potential vxc computed before (xc_eval), with the sums of k_xc_veff
+// except [0] = rho e_xc W (erho = rho_c e_xc) and [1] = 0, so that Exc = [0] - C2 [1] holds for
+// every functional.
+__global__ void k_veff_sums(const double* __restrict__ rho, const double* __restrict__ phi, const double* __restrict__ b,
+                            const double* __restrict__ W, const double* __restrict__ veff_in, const double* __restrict__ vxc,
+                            const double* __restrict__ erho, double* __restrict__ veff, int N, double* __restrict__ partial) {
+  double s[kNSums] = {0, 0, 0, 0, 0, 0, 0};
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) {
+    const double r0 = rho[p];
+    const double rc = r0 < kXcRhoTol ? kXcRhoTol : r0;
+    const double v = vxc[p];
+    const double ve = phi[p] + v;
+    veff[p] = ve;
+    const double w = W[p];
+    const double d = ve - veff_in[p];
+    s[0] += erho[p] * w;
+    s[2] += v * rc * w;
+    s[3] += (b[p] - r0) * phi[p] * w;
+    s[4] += d * r0 * w;
+    s[5] += d * d;
+    s[6] += ve * ve;
   }
-  __syncthreads();
-  if (threadIdx.x < kNSums) {
-    double t = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[threadIdx.x][w];
-    partial[(size_t)blockIdx.x * kNSums + threadIdx.x] = t;
+  block_partials(s, partial);
+}
+
+// ---- exchange-correlation potentials on their own (LDA_PW, LDA_PZ, GGA_PBE), for xc_eval
+// vxc = d(rho e_xc)/d rho and erho = rho_c e_xc at the clipped density
+template <int XC>
+__global__ void k_xc_lda(const double* __restrict__ rho, int N, double* __restrict__ vxc, double* __restrict__ erho) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) {
+    const double r0 = rho[p];
+    const double rc = r0 < kXcRhoTol ? kXcRhoTol : r0;
+    double v, e;
+    if (XC == xc::kLdaPw) {
+      xc::lda_pw(rc, v, e);
+      e = e * rc - 0.73855876638202 * rc * cbrt(rc);
+    } else {
+      xc::lda_pz(rc, v, e);
+    }
+    vxc[p] = v;
+    erho[p] = e;
+  }
+}
+
+// GGA_PBE in two passes over the grid (the per-point arithmetic is xc::gga_pass1_point /
+// gga_pass2_point): the flux q of every point must be complete before its divergence is taken.
+__global__ void k_gga_pass1(const double* __restrict__ rho, xc::GgaGrid g, int N, double* __restrict__ vxc,
+                            double* __restrict__ erho, double* __restrict__ q) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) xc::gga_pass1_point(rho, g, p, vxc, erho, q);
+}
+
+__global__ void k_gga_pass2(const double* __restrict__ q, xc::GgaGrid g, int N, double* __restrict__ vxc) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) xc::gga_pass2_point(q, g, p, vxc);
+}
+
+// e_xc = erho / rho_c (the energy per particle that exchangeCorrelationPotential stores in S.e_xc)
+__global__ void k_exc_per_particle(const double* __restrict__ rho, int N, double* __restrict__ erho) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < N; p += gridDim.x * blockDim.x) {
+    const double r0 = rho[p];
+    erho[p] /= r0 < kXcRhoTol ? kXcRhoTol : r0;
   }
 }
 
@@ -216,6 +279,7 @@ __global__ void k_to_float(const double* __restrict__ a, float* __restrict__ b, 
 
 struct ScfBufs {
   double *rho, *b, *phi, *vxc, *vin, *f, *X, *F, *xkm1, *fkm1, *fk, *partial, *sums, *ev, *occ, *wst, *occout, *io;
+  double *erho, *q;          // rho e_xc (N) and the GGA flux 2 df/dsigma grad rho (3 N)
   int nred;
 };
 
@@ -260,6 +324,49 @@ cx_status eigsolver_dispatch(cx_handle h, int count, int npl, int rhoTrigger, do
 
 static unsigned grid_n(int N) { return (unsigned)std::min(152 * 8, (N + 255) / 256); }
 
+// Vxc and rho e_xc of the functional xc on the device density rho (N each); q: 3 N work values
+// for GGA_PBE.  Launches on the handle's stream.
+static cx_status xc_eval(cx_handle h, int xc, const double* rho, double* vxc, double* erho, double* q) {
+  const int N = h->g.N;
+  const unsigned gN = grid_n(N);
+  const cudaStream_t st = h->stream;
+  if (xc == xc::kLdaPw) {
+    k_xc_lda<xc::kLdaPw><<<gN, 256, 0, st>>>(rho, N, vxc, erho);
+    h->launches++;
+  } else if (xc == xc::kLdaPz) {
+    k_xc_lda<xc::kLdaPz><<<gN, 256, 0, st>>>(rho, N, vxc, erho);
+    h->launches++;
+  } else {
+    xc::GgaGrid g{};
+    g.Nx = h->g.Nx; g.Ny = h->g.Ny; g.Nz = h->g.Nz; g.FDn = h->g.FDn;
+    g.xin = h->grid.xin; g.dx = h->grid.dx; g.dy = h->grid.dy; g.dz = h->grid.dz; g.twist = h->grid.twist;
+    for (int k = 1; k <= h->g.FDn; ++k) {
+      g.gr[k] = h->w1[k] / h->grid.dx;
+      g.gt[k] = h->w1[k] / h->grid.dy;
+      g.gz[k] = h->w1[k] / h->grid.dz;
+    }
+    k_gga_pass1<<<gN, 256, 0, st>>>(rho, g, N, vxc, erho, q);
+    k_gga_pass2<<<gN, 256, 0, st>>>(q, g, N, vxc);
+    h->launches += 2;
+  }
+  CX_TRY_CUDA(h, cudaGetLastError());
+  return CX_OK;
+}
+
+// the functionals cx_scf and cx_xc accept on the handle's grid
+static bool xc_supported(cx_handle h, int xc) {
+  if (xc == xc::kLdaPw || xc == xc::kLdaPz) return true;
+  if (xc != xc::kGgaPbe) {
+    h->err = "exchange-correlation code " + std::to_string(xc) + ": 0 LDA_PW, 1 LDA_PZ or 2 GGA_PBE";
+    return false;
+  }
+  if (h->grid.BCy != 0 || h->grid.BCz != 0) {
+    h->err = "GGA_PBE: the gradient stencils need periodic theta and z (BCy = BCz = 0)";
+    return false;
+  }
+  return true;
+}
+
 // phi = Poisson(rho), Vxc(rho), Veff = phi + Vxc (into h->d_veff) and the energy / error sums
 static cx_status scf_potential(cx_handle h, ScfState& S, int use_guess, int* iters, float* pms) {
   const int N = h->g.N;
@@ -274,7 +381,13 @@ static cx_status scf_potential(cx_handle h, ScfState& S, int use_guess, int* ite
   cx_status s = poisson_dev(h, B.f, B.phi, S.ptol, S.pmax, use_guess, &it, &rr);
   if (s != CX_OK && s != CX_ERR_NOCONV) return s;
   CX_TRY_CUDA(h, cudaEventRecord(S.p1, st));
-  k_xc_veff<<<gN, 256, 0, st>>>(B.rho, B.phi, B.b, h->d_W, B.vin, B.vxc, h->d_veff, N, B.partial);
+  if (S.P.xc == xc::kLdaPw) {
+    k_xc_veff<<<gN, 256, 0, st>>>(B.rho, B.phi, B.b, h->d_W, B.vin, B.vxc, h->d_veff, N, B.partial);
+  } else {
+    cx_status xs = xc_eval(h, S.P.xc, B.rho, B.vxc, B.erho, B.q);
+    if (xs != CX_OK) return xs;
+    k_veff_sums<<<gN, 256, 0, st>>>(B.rho, B.phi, B.b, h->d_W, B.vin, B.vxc, B.erho, h->d_veff, N, B.partial);
+  }
   k_sum_partials<<<1, 32 * kNSums, 0, st>>>(B.partial, (int)gN, kNSums, B.sums);
   h->launches += 2;
   CX_TRY_CUDA(h, cudaMemcpyAsync(S.sums, B.sums, sizeof(S.sums), cudaMemcpyDeviceToHost, st));
@@ -310,6 +423,7 @@ extern "C" cx_status cx_scf_init(cx_handle h, const cx_scf_params* P) {
   if (!P) { h->err = "cx_scf_init: null parameters"; return CX_ERR_ARG; }
   if (h->nblk < 1) { h->err = "cx_scf: call cx_set_blocks (and cx_set_psi) first"; return CX_ERR_STATE; }
   if (h->nspin != 1) { h->err = "cx_scf: the SCF driver supports nspin = 1 (spin blocks are supported by cx_eigsolver)"; return CX_ERR_ARG; }
+  if (!xc_supported(h, P ? P->xc : 0)) { h->err = "cx_scf: " + h->err; return CX_ERR_ARG; }
   if (!P->b || !P->rho0 || !P->wkpt || P->max_scf < 1 || P->npl < 1 || !(P->scf_tol > 0) || !(P->bet > 0)) {
     h->err = "cx_scf: need b, rho0, wkpt, max_scf >= 1, npl >= 1, scf_tol > 0, bet > 0";
     return CX_ERR_ARG;
@@ -330,7 +444,7 @@ extern "C" cx_status cx_scf_init(cx_handle h, const cx_scf_params* P) {
   // ---- device buffers
   ScfBufs& B = S->B;
   B.nred = (int)gN;
-  const size_t need = (size_t)N * 8 * (9 + 2 * m) + (size_t)gN * kNSums * 8 + 64 * 8 + (size_t)ntot * 8 * 3 + 8 * (m * m + 2 * m + 8) +
+  const size_t need = (size_t)N * 8 * (13 + 2 * m) + (size_t)gN * kNSums * 8 + 64 * 8 + (size_t)ntot * 8 * 3 + 8 * (m * m + 2 * m + 8) +
                       64 * 256;
   if (h->scf_bytes < need) {
     cudaFree(h->d_scf);
@@ -347,6 +461,7 @@ extern "C" cx_status cx_scf_init(cx_handle h, const cx_scf_params* P) {
     B.fk = take((size_t)N * 8); B.X = take((size_t)N * 8 * m); B.F = take((size_t)N * 8 * m);
     B.partial = take((size_t)gN * kNSums * 8); B.sums = take(64 * 8); B.ev = take((size_t)ntot * 8); B.occ = take((size_t)ntot * 8);
     B.wst = take((size_t)ntot * 8); B.occout = take(8 * 8); B.io = take(8 * (m * m + 2 * m + 8));
+    B.erho = take((size_t)N * 8); B.q = take((size_t)N * 8 * 3);
   }
   S->wblk.assign(P->wkpt, P->wkpt + nblk);
   std::vector<double> wst(ntot);
@@ -540,4 +655,36 @@ extern "C" cx_status cx_scf(cx_handle h, const cx_scf_params* P, double* EigVal,
     for (size_t i = 0; i < S.hist.size() && i < cap; ++i) hist[i] = S.hist[i];
   }
   return cx_scf_finish(h, EigVal, rho_out, Veff_out, res);
+}
+
+extern "C" cx_status cx_xc(cx_handle h, int32_t xc, const double* rho, double* Vxc, double* e_xc) {
+  if (!h) return CX_ERR_ARG;
+  if (!rho || !Vxc || !e_xc) { h->err = "cx_xc: rho, Vxc and e_xc are required"; return CX_ERR_ARG; }
+  if (!xc_supported(h, xc)) { h->err = "cx_xc: " + h->err; return CX_ERR_ARG; }
+  const int N = h->g.N;
+  const cudaStream_t st = h->stream;
+  double* d = nullptr;                       // rho, Vxc, rho e_xc, 3 N GGA work values
+  if (cudaMalloc(&d, (size_t)N * 8 * 6) != cudaSuccess) {
+    cudaGetLastError();
+    h->err = "cx_xc: device allocation failed";
+    return CX_ERR_NOMEM;
+  }
+  double *d_rho = d, *d_vxc = d + N, *d_e = d + 2 * (size_t)N, *d_q = d + 3 * (size_t)N;
+  cx_status s = CX_OK;
+  cudaError_t e = cudaMemcpyAsync(d_rho, rho, (size_t)N * 8, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) s = xc_eval(h, xc, d_rho, d_vxc, d_e, d_q);
+  if (e == cudaSuccess && s == CX_OK) {
+    k_exc_per_particle<<<grid_n(N), 256, 0, st>>>(d_rho, N, d_e);
+    h->launches++;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && s == CX_OK) e = cudaMemcpyAsync(Vxc, d_vxc, (size_t)N * 8, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && s == CX_OK) e = cudaMemcpyAsync(e_xc, d_e, (size_t)N * 8, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(d);
+  if (e != cudaSuccess) {
+    h->err = std::string("cx_xc: ") + cudaGetErrorString(e);
+    return CX_ERR_CUDA;
+  }
+  return s;
 }

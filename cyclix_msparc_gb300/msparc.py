@@ -7,6 +7,8 @@ reference project root ``Cyclix_MS_200220/``):
 * ``chebyshev_filter(X,m,a,b,a0,DL11,DL22,DL33,DG1,DG2,DG3,Veff,S,kpt_vec)``  src/chebyshev_filter.m:1
 * ``eigSolver(S,count,upper_bound_guess_vecs,psi,EigVal,a0,bup,lambda_cutoff)``  src/eigSolver.m:1
 * ``poissonSolve(S,poisson_tol,Isguess)``  src/poissonSolve.m:1
+* ``exchangeCorrelationPotential(S)`` (nspin = 1)  src/exchangeCorrelationPotential.m:1
+* ``scf(S)``  src/scf.m:1
 
 MATLAB hands the six 1-D operators to the first two; on the GPU the operator is rebuilt from
 the grid in ``S`` and the Bloch vector, so those arguments are accepted and not read.  The GPU
@@ -23,7 +25,8 @@ from . import _lib
 from ._lib import CxError, check, cptr, dptr
 from .cychel import split_projector_columns
 
-__all__ = ["CyclixGPU", "attach", "h_nonlocal_vector_mult", "chebyshev_filter", "eigSolver", "poissonSolve", "scf", "CxError"]
+__all__ = ["CyclixGPU", "attach", "h_nonlocal_vector_mult", "chebyshev_filter", "eigSolver", "poissonSolve",
+           "exchangeCorrelationPotential", "scf", "CxError"]
 
 
 def _host_buffer(a, dtype, size: int, name: str) -> None:
@@ -188,9 +191,7 @@ class CyclixGPU:
                                                                 dptr(EigVal), dptr(a0), dptr(bup), dptr(lambda_cutoff)))
 
     def _scf_params(self, S, scf_tol, poisson_tol, max_scf, min_scf, rhoTrigger, maxit_poisson, mixing_param, refine, fp64_tol=0.0):
-        xc = S.extra.get("xc", "LDA_PW") if hasattr(S, "extra") else "LDA_PW"
-        if xc != "LDA_PW":
-            raise CxError(_lib.CX_ERR_ARG, f"cx_scf implements LDA_PW, not {xc}")
+        xc = self._xc_code(S)
         wk = np.ascontiguousarray([S.wkpt[i % S.tnkpt] for i in range(len(self.blocks))], dtype=np.float64)
         b = np.ascontiguousarray(S.b, dtype=np.float64)
         rho0 = np.ascontiguousarray(S.rho_at, dtype=np.float64)
@@ -198,8 +199,30 @@ class CyclixGPU:
                                npl=int(S.npl), maxit_poisson=maxit_poisson, elec_T_type=int(S.elec_T_type), bet=float(S.bet),
                                occfac=float(S.occfac), NegCharge=float(S.NegCharge), Eself=float(S.Eself), E_corr=float(S.E_corr),
                                n_atm=int(S.n_atm), mixing_param=mixing_param, wkpt=dptr(wk), b=dptr(b), rho0=dptr(rho0),
-                               refine=int(self.prec == "mixed" if refine is None else refine), fp64_tol=float(fp64_tol))
+                               refine=int(self.prec == "mixed" if refine is None else refine), fp64_tol=float(fp64_tol),
+                               xc=xc)
         return p, (wk, b, rho0)
+
+    @staticmethod
+    def _xc_code(S):
+        """The CX_XC_* code of the system's functional (S.XC, held in ``S.extra['xc']``; LDA_PW by default)."""
+        name = S.extra.get("xc", "LDA_PW") if hasattr(S, "extra") else "LDA_PW"
+        if name not in _lib.XC:
+            raise CxError(_lib.CX_ERR_ARG, f"exchange-correlation {name}: the library implements {', '.join(_lib.XC)}")
+        return _lib.XC[name]
+
+    def xc(self, rho, xc="LDA_PW"):
+        """(Vxc, e_xc) of ``exchangeCorrelationPotential`` for nspin = 1 on the density ``rho`` (cx_xc):
+        e_xc is the energy per particle at the density clipped at 1e-14."""
+        rho = np.ascontiguousarray(rho, dtype=np.float64).reshape(-1)
+        if rho.size != self.N:
+            raise ValueError(f"xc: rho needs N = {self.N} values, got {rho.size}")
+        if xc not in _lib.XC:
+            raise CxError(_lib.CX_ERR_ARG, f"exchange-correlation {xc}: the library implements {', '.join(_lib.XC)}")
+        V = np.zeros(self.N)
+        e = np.zeros(self.N)
+        check(self.lib, self.h, self.lib.cx_xc(self.h, _lib.XC[xc], dptr(rho), dptr(V), dptr(e)))
+        return V, e
 
     def scf(self, S, scf_tol=1e-6, poisson_tol=-1.0, max_scf=100, min_scf=3, rhoTrigger=4, maxit_poisson=1000,
             mixing_param=0.3, refine=None, fp64_tol=0.0):
@@ -414,6 +437,14 @@ def scf(S, scf_tol=1e-6):
     S.Etotal, S.EigVal, S.lambda_f, S.rho = res.Etotal, EV, res.lambda_f, rho
     S.Veff = V.reshape(-1, 1)
     S.extra["scf"] = dict(n_scf=res.n_scf, converged=bool(res.converged), err=res.err, history=hist)
+    return S
+
+
+def exchangeCorrelationPotential(S):
+    """``S = exchangeCorrelationPotential(S)`` for nspin = 1 (src/exchangeCorrelationPotential.m:1-80):
+    ``S.Vxc`` and ``S.e_xc`` of ``S.rho`` for the functional ``S.extra['xc']`` (LDA_PW, LDA_PZ or GGA_PBE)."""
+    rho = np.asarray(S.rho).reshape(S.N, -1, order="F")[:, 0]
+    S.Vxc, S.e_xc = S.gpu.xc(rho, S.extra.get("xc", "LDA_PW"))
     return S
 
 

@@ -16,6 +16,8 @@
  *                         src/poissonSolve.m:1, src/aar.m:1
  *   cx_scf              S = scf(S): the SCF loop around eigSolver (first relaxation step,
  *                         nspin = 1, potential mixing) src/scf.m:1-327
+ *   cx_xc               S = exchangeCorrelationPotential(S) (nspin = 1: LDA_PW, LDA_PZ, GGA_PBE)
+ *                         src/exchangeCorrelationPotential.m:1-80
  *
  * The operator data that MATLAB keeps in the struct S (grid, FD weights,
  * quadrature weights, KB projector images) is handed over once in cx_create;
@@ -203,7 +205,24 @@ cx_status cx_poisson(cx_handle h, const double* f, double* phi, double tol, int3
  * completely written (the caller synchronises the stream that wrote it) before the call. */
 cx_status cx_hpsi_noalloc(cx_handle h, int32_t blk, int32_t ncol, const void* X_dev, void* Y_dev, int32_t prec);
 
-/* SCF parameters: the S fields read by src/scf.m (nspin = 1, LDA_PW, potential mixing). */
+/* Exchange-correlation functional: the reference's S.xc codes (src/initialization.m:145-154). */
+enum {
+  CX_XC_LDA_PW = 0,      /* Perdew-Wang 1992 LDA (src/exchangeCorrelationPotential.m:82-106) */
+  CX_XC_LDA_PZ = 1,      /* Perdew-Zunger 1981 LDA (src/evaluateTotalEnergy.m:44-60) */
+  CX_XC_GGA_PBE = 2      /* PBE GGA on the Cyclix gradients (src/exchangeCorrelationPotential.m:156-362) */
+};
+
+/* S = exchangeCorrelationPotential(S) for nspin = 1 on the density rho (N, host): Vxc (N) and
+ * e_xc (N), the energy per particle at the density clipped below at 1e-14 (S.xc_rhotol), so that
+ * Exc = sum(e_xc .* max(rho, 1e-14) .* W) (src/evaluateTotalEnergy.m:25-62).  xc is a CX_XC_*
+ * code.  GGA_PBE differentiates the clipped density with the order-2 FDn first-derivative
+ * stencils of the Cyclix grid (Cartesian components through the local angle theta + twist z,
+ * Cychel/gradIndicesValues_cychel.m) and forms Vxc = d(rho e_xc)/d rho - div(2 d(rho e_xc)/d sigma
+ * grad rho) with the same operators (src/exchangeCorrelationPotential.m:354-362); it needs theta
+ * and z periodic.  Allocates and frees its device work arrays. */
+cx_status cx_xc(cx_handle h, int32_t xc, const double* rho, double* Vxc, double* e_xc);
+
+/* SCF parameters: the S fields read by src/scf.m (nspin = 1, potential mixing). */
 typedef struct {
   double scf_tol;            /* S.SCF_tol: stop when ||Veff - Veff_in|| / ||Veff|| <= scf_tol */
   double poisson_tol;        /* S.poisson_tol (<= 0: 0.01 * scf_tol, src/initialization.m:548-552) */
@@ -227,6 +246,8 @@ typedef struct {
                                 switch the blocks to complex128 (psi converted) and continue with FP64
                                 passes until the error is <= fp64_tol (at most max_scf more): the fixed
                                 point of the reference's arithmetic.  The blocks stay complex128. */
+  int32_t xc;                /* S.xc: CX_XC_LDA_PW (0, the value of a zeroed struct), CX_XC_LDA_PZ or
+                                CX_XC_GGA_PBE; the potential and energy of every SCF step use it */
 } cx_scf_params;
 
 typedef struct {
@@ -238,7 +259,7 @@ typedef struct {
 } cx_scf_result;
 
 /* S = scf(S) (src/scf.m:1-327) on the device-resident psi of the handle's blocks: initial
- * potential from rho0, then eigSolver / occupations / density / Poisson / LDA_PW / energy /
+ * potential from rho0, then eigSolver / occupations / density / Poisson / Vxc (p->xc) / energy /
  * Periodic-Pulay potential mixing until converged.  EigVal (packed, sum Ns), rho (N), Veff (N)
  * and hist (max_scf x 2, or 2 max_scf x 2 with p->fp64_tol > 0: energy per atom, error per SCF
  * step) are outputs (rho, Veff, hist may be NULL). */
@@ -248,7 +269,7 @@ cx_status cx_scf(cx_handle h, const cx_scf_params* p, double* EigVal, double* rh
 /* One SCF step at a time: the same loop as cx_scf, driven by the caller (src/scf.m:111-306).
  * cx_scf_init sets the initial potential from p->rho0 (src/scf.m:32-39); each cx_scf_step is
  * one pass of the loop body: the eigSolver step, occupations and, once count >= rhoTrigger, the
- * density, Poisson solve, LDA_PW potential, energy, error and Pulay mixing; cx_scf_finish
+ * density, Poisson solve, exchange-correlation potential, energy, error and Pulay mixing; cx_scf_finish
  * applies the optional FP64 refinement and returns the results (EigVal, rho, Veff may be NULL).
  * The caller stops when info.converged is set or its step limit is reached, as src/scf.m:111. */
 typedef struct {

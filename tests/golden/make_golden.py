@@ -26,7 +26,7 @@ for p in (ROOT, ROOT / "tests"):
         sys.path.insert(0, str(p))
 
 from cyclix_msparc_gb300.workloads import WORKLOADS, block_layout, initial_psi, make_system  # noqa: E402
-from kat_systems import tiny_cyclic_workload, tiny_helical_workload  # noqa: E402
+from kat_systems import tiny_cyclic_workload, tiny_helical_workload, xc_density  # noqa: E402
 from oracle import cychel_ops as O  # noqa: E402
 
 # filter parameters of the fixtures: degree, cutoff, upper bound, lower bound
@@ -91,18 +91,41 @@ def poisson_case() -> dict:
     return dict(phi=phi, relres=relres, iters=it)
 
 
-def scf_small(name: str = "scf-small-24x12x20-12at-2k-ns40", fermi_dirac: bool = False) -> dict:
+def xc_case(name: str) -> dict:
+    """Vxc and e_xc of LDA_PW, LDA_PZ and GGA_PBE (src/exchangeCorrelationPotential.m, nspin = 1)
+    on xc_density(S, 17) of a workload's grid; e_xc per particle at the clipped density."""
+    from oracle.scf import XC_RHOTOL, cyclix_gradients, gga_pbe, lda_pw_potential, lda_pz_potential, _pz_corr
+    S = make_system(WORKLOADS[name])
+    rho = xc_density(S, 17)
+    rc = np.where(rho < XC_RHOTOL, XC_RHOTOL, rho)
+    out = {}
+    out["V_LDA_PW"] = lda_pw_potential(rho)
+    rs = (0.75 / (np.pi * rc)) ** (1 / 3)
+    A, a1 = 0.031091, 0.21370
+    b1, b2, b3, b4 = 7.5957, 3.5876, 1.6382, 0.49294
+    ec = -2 * A * (1 + a1 * rs) * np.log(1 + 1 / (2 * A * (b1 * rs ** 0.5 + b2 * rs + b3 * rs ** 1.5 + b4 * rs * rs)))
+    C2 = 0.73855876638202
+    out["e_LDA_PW"] = ec - C2 * rc ** (1 / 3)
+    out["V_LDA_PZ"] = lda_pz_potential(rho)
+    out["e_LDA_PZ"] = _pz_corr(rc)[0] - C2 * rc ** (1 / 3)
+    V, e = gga_pbe(rho, cyclix_gradients(S))
+    out["V_GGA_PBE"], out["e_GGA_PBE"] = V, e
+    return out
+
+
+def scf_small(name: str = "scf-small-24x12x20-12at-2k-ns40", fermi_dirac: bool = False, xc: str = "LDA_PW") -> dict:
     """The oracle SCF (src/scf.m) on a small cell, tol 1e-6, psi = initial_psi(N, Ns, 7 + b);
-    Gaussian smearing, or Fermi-Dirac at the same smearing width."""
+    Gaussian smearing, or Fermi-Dirac at the same smearing width; exchange-correlation xc."""
     wl = WORKLOADS[name]
     S = make_system(wl)
     if fermi_dirac:
         S.elec_T_type = 0
+    S.extra["xc"] = xc
     bl = block_layout(wl, S)
     psis = [initial_psi(S.N, n, 7 + i) for i, (_, _, n) in enumerate(bl)]
     from oracle.scf import scf
     r = scf(S, psis, bl, scf_tol=1e-6)
-    return dict(workload=wl.name, smearing="fermi-dirac" if fermi_dirac else "gaussian", scf_tol=1e-6, n_atm=S.n_atm,
+    return dict(workload=wl.name, smearing="fermi-dirac" if fermi_dirac else "gaussian", xc=xc, scf_tol=1e-6, n_atm=S.n_atm,
                 Etotal=r["Etotal"], E_per_atom=r["Etotal"] / S.n_atm,
                 lambda_f=r["lambda_f"], n_scf=r["n_scf"], history=[list(h) for h in r["history"]],
                 EigVal=[ev.tolist() for ev in r["EigVal"]])
@@ -120,6 +143,15 @@ def write_all(which=None):
             json.dumps(scf_small("scf-small-helical-24x12x16-8at-2k-ns28"), indent=1)),
         "scf_small_fd": lambda: (HERE / "scf_small_fd.json").write_text(
             json.dumps(scf_small(fermi_dirac=True), indent=1)),
+        "scf_small_gga": lambda: (HERE / "scf_small_gga.json").write_text(
+            json.dumps(scf_small(xc="GGA_PBE"), indent=1)),
+        "scf_small_helical_gga": lambda: (HERE / "scf_small_helical_gga.json").write_text(
+            json.dumps(scf_small("scf-small-helical-24x12x16-8at-2k-ns28", xc="GGA_PBE"), indent=1)),
+        "scf_small_pz": lambda: (HERE / "scf_small_pz.json").write_text(
+            json.dumps(scf_small(xc="LDA_PZ"), indent=1)),
+        "xc_cyclic": lambda: np.savez_compressed(HERE / "xc_cyclic.npz", **xc_case("scf-small-24x12x20-12at-2k-ns40")),
+        "xc_helical": lambda: np.savez_compressed(HERE / "xc_helical.npz",
+                                                  **xc_case("scf-small-helical-24x12x16-8at-2k-ns28")),
     }
     for k, fn in jobs.items():
         if which is None or k in which:

@@ -45,3 +45,19 @@ def tiny_helical_workload():
     from cyclix_msparc_gb300.workloads import Workload
     return Workload("helical-tiny-16x8x10", 16, 8, 10, (6, 6), ((0.0, 1.0, 0.0), (0.0, 0.0, 0.9)), 1, 6, 2, 4,
                     twist=0.05, L1=4.0, xin=4.0)
+
+
+def xc_density(S, seed: int) -> np.ndarray:
+    """A positive density with structure on every axis: the atomic superposition times a seeded
+    smooth modulation, plus a seeded 2 % noise; 1 % of the points set to zero or below the 1e-14
+    clip (the clipped branch of src/exchangeCorrelationPotential.m)."""
+    rng = np.random.default_rng(seed)
+    r = np.asarray(S.rho_at, dtype=np.float64).reshape(-1)
+    i = np.arange(S.N)
+    th = (i // S.Nx) % S.Ny * (2 * np.pi / S.Ny)
+    z = i // (S.Nx * S.Ny) * (2 * np.pi / S.Nz)
+    rho = np.abs(r) * (1.0 + 0.3 * np.sin(th + rng.uniform(0, 2 * np.pi)) * np.cos(z + rng.uniform(0, 2 * np.pi)))
+    rho *= 1.0 + 0.02 * rng.standard_normal(S.N)
+    low = rng.choice(S.N, S.N // 100, replace=False)
+    rho[low] = rng.choice([0.0, 1e-16, -1e-12], low.size)
+    return rho

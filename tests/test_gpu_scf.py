@@ -1,6 +1,6 @@
 """GPU SCF (cx_scf, src/scf.m) against the oracle SCF fixtures: the cyclic 24 x 12 x 20 12-atom cell
-(Gaussian and Fermi-Dirac smearing, src/occupations.m) and the helical (twist 0.05 rad/bohr)
-24 x 12 x 16 8-atom cell.
+(Gaussian and Fermi-Dirac smearing, src/occupations.m; LDA_PW, LDA_PZ and GGA_PBE) and the helical
+(twist 0.05 rad/bohr) 24 x 12 x 16 8-atom cell (LDA_PW and GGA_PBE).
 
 Tolerances:
   * complex128: total energy within 1e-7 Ha/atom of the oracle, Fermi level within 1e-5 Ha and
@@ -26,7 +26,10 @@ GOLD = Path(__file__).resolve().parent / "golden"
 
 CASES = [("scf-small-24x12x20-12at-2k-ns40", "scf_small.json", 24),
          ("scf-small-helical-24x12x16-8at-2k-ns28", "scf_small_helical.json", 16),
-         ("scf-small-24x12x20-12at-2k-ns40", "scf_small_fd.json", 24)]
+         ("scf-small-24x12x20-12at-2k-ns40", "scf_small_fd.json", 24),
+         ("scf-small-24x12x20-12at-2k-ns40", "scf_small_gga.json", 24),
+         ("scf-small-helical-24x12x16-8at-2k-ns28", "scf_small_helical_gga.json", 16),
+         ("scf-small-24x12x20-12at-2k-ns40", "scf_small_pz.json", 24)]
 
 
 @pytest.fixture(scope="module", params=CASES, ids=[c[1].split(".")[0] for c in CASES])
@@ -37,6 +40,7 @@ def scf_system(request):
     ref = json.loads((GOLD / fixture).read_text())
     if ref.get("smearing") == "fermi-dirac":
         S.elec_T_type = 0
+    S.extra["xc"] = ref.get("xc", "LDA_PW")
     return wl, S, block_layout(wl, S), ref, nocc
 
 
