@@ -8,7 +8,8 @@ psp8 projectors in the S.Atom(J).rcImage layout) is saved as ``deck_<name>.npz``
 script, with the free energy per atom of the deck's ``.out`` file and the tolerances of its run.
 Nothing of the reference's files is copied: the arrays are this library's set-up of the deck.
 
-    CYCLIX_REFERENCE=<reference project root> python tests/golden/make_deck_fixtures.py
+    CYCLIX_REFERENCE=<reference project root> python tests/golden/make_deck_fixtures.py [name ...]
+    python tests/golden/make_deck_fixtures.py --oracle GGA_wrong_SG15   # tight oracle SCF of a saved deck
 """
 import os
 import sys
@@ -19,7 +20,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path[:0] = [ROOT, os.path.join(ROOT, "tests")]
 
-DECKS = {"CNT_chiral": "tests/Cyclix/CNT_chiral/C.inpt", "CNT_ABINITmatch": "tests/Cyclix/CNT_ABINITmatch/C.inpt"}
+DECKS = {"CNT_chiral": "tests/Cyclix/CNT_chiral/C.inpt", "CNT_ABINITmatch": "tests/Cyclix/CNT_ABINITmatch/C.inpt",
+         "GGA_wrong_SG15": "GGA_wrong_SG15/C.inpt"}
 
 
 def save(name, rel, root):
@@ -43,6 +45,7 @@ def save(name, rel, root):
         img_nnodes=np.array([img.rc_pos.size for A in S.Atom for img in A.rcImage], dtype=np.int64),
         img_pos=np.concatenate([img.rc_pos for A in S.Atom for img in A.rcImage]).astype(np.int32),
         img_chi=np.concatenate([img.Chi_mat.reshape(-1, order="F") for A in S.Atom for img in A.rcImage]),
+        xc=np.array(S.extra.get("xc", "LDA_PW")),
     )
     path = os.path.join(HERE, f"deck_{name}.npz")
     np.savez_compressed(path, **arrays)
@@ -78,13 +81,42 @@ def load(name):
     S.b, S.rho_at = z["b"], z["rho_at"]
     S.NegCharge, S.Eself, S.E_corr, S.bet = float(NegCharge), float(Eself), float(E_corr), float(bet)
     S.elec_T_type, S.occfac, S.n_atm = int(elec_T_type), float(occfac), int(n_atm)
-    S.extra.update(deck=name, xc="LDA_PW")
+    S.extra.update(deck=name, xc=str(z["xc"]) if "xc" in z.files else "LDA_PW")
     return S, float(scf_tol), float(poisson_tol), float(e_ref)
 
 
+def oracle_reference(name, scf_tol=1e-8, poisson_tol=1e-10, max_scf=60):
+    """The oracle SCF (oracle/scf.py) on the saved set-up of a deck, from the initial psi the GPU
+    deck tests use (initial_psi(N, Nev, 700 + b)), converged tightly so that the fixed point does not
+    depend on the Poisson solver's stopping point; written to deck_<name>_oracle.json."""
+    import json
+    import time
+    from cyclix_msparc_gb300.workloads import initial_psi
+    from oracle.scf import scf
+    S, _, _, e_ref = load(name)
+    blocks = [(S.kptgrid[k].copy(), 0, S.Nev) for k in range(S.tnkpt)]
+    psis = [initial_psi(S.N, S.Nev, 700 + b) for b in range(len(blocks))]
+    t = time.time()
+    r = scf(S, psis, blocks, scf_tol=scf_tol, poisson_tol=poisson_tol, max_scf=max_scf,
+            log=lambda c, e, err: print(f"{name} oracle SCF {c}: {e:.12f} Ha/atom, error {err:.3e}", flush=True))
+    out = dict(deck=name, xc=S.extra["xc"], scf_tol=scf_tol, poisson_tol=poisson_tol, n_scf=r["n_scf"],
+               free_energy_per_atom=r["Etotal"] / S.n_atm, lambda_f=r["lambda_f"], printed_free_energy_per_atom=e_ref,
+               history=[list(h) for h in r["history"]], wall_s=round(time.time() - t, 1))
+    path = os.path.join(HERE, f"deck_{name}_oracle.json")
+    with open(path, "w") as f:
+        json.dump(out, f, indent=1)
+    print(f"{name}: oracle {out['free_energy_per_atom']:.12f} Ha/atom after {out['n_scf']} steps -> {path}")
+
+
 if __name__ == "__main__":
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    if "--oracle" in sys.argv:
+        for name in args:
+            oracle_reference(name)
+        sys.exit(0)
     root = os.environ.get("CYCLIX_REFERENCE", "")
     if not root:
         sys.exit("set CYCLIX_REFERENCE to the reference project root")
     for name, rel in DECKS.items():
-        save(name, rel, root)
+        if not args or name in args:
+            save(name, rel, root)
