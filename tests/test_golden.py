@@ -40,13 +40,40 @@ def test_poisson_golden():
     assert np.max(np.abs(out["phi"] - ref["phi"])) <= 1e-9 * np.max(np.abs(ref["phi"]))
 
 
+@pytest.mark.parametrize("name,fixture", [("scf-small-24x12x20-12at-2k-ns40", "xc_cyclic.npz"),
+                                          ("scf-small-helical-24x12x16-8at-2k-ns28", "xc_helical.npz")],
+                         ids=["cyclic", "helical"])
+def test_xc_golden(name, fixture):
+    ref = np.load(GOLD / fixture)
+    out = G.xc_case(name)
+    assert sorted(out) == sorted(ref.files)
+    for k in ref.files:
+        assert np.max(np.abs(out[k] - ref[k])) <= 1e-13 * np.max(np.abs(ref[k])), k
+
+
+def test_gga_deck_oracle_record():
+    """The oracle's tight SCF of the GGA_wrong_SG15 set-up: converged to its tolerance, for the
+    deck's functional, with the printed energy of the saved set-up."""
+    from golden.make_deck_fixtures import load
+    rec = json.loads((GOLD / "deck_GGA_wrong_SG15_oracle.json").read_text())
+    S, _, _, e_ref = load("GGA_wrong_SG15")
+    assert rec["xc"] == S.extra["xc"] == "GGA_PBE"
+    assert rec["history"][-1][2] <= rec["scf_tol"]
+    assert rec["printed_free_energy_per_atom"] == e_ref
+    assert abs(rec["history"][-1][1] - rec["free_energy_per_atom"]) < 1e-12
+    assert abs(rec["free_energy_per_atom"] - e_ref) < 3e-6
+
+
 @pytest.mark.slow
 @pytest.mark.parametrize("name,fixture", [("scf-small-24x12x20-12at-2k-ns40", "scf_small.json"),
                                           ("scf-small-helical-24x12x16-8at-2k-ns28", "scf_small_helical.json"),
-                                          ("scf-small-24x12x20-12at-2k-ns40", "scf_small_fd.json")])
+                                          ("scf-small-24x12x20-12at-2k-ns40", "scf_small_fd.json"),
+                                          ("scf-small-24x12x20-12at-2k-ns40", "scf_small_gga.json"),
+                                          ("scf-small-helical-24x12x16-8at-2k-ns28", "scf_small_helical_gga.json"),
+                                          ("scf-small-24x12x20-12at-2k-ns40", "scf_small_pz.json")])
 def test_scf_golden(name, fixture):
     ref = json.loads((GOLD / fixture).read_text())
-    out = G.scf_small(name, fermi_dirac=ref.get("smearing") == "fermi-dirac")
+    out = G.scf_small(name, fermi_dirac=ref.get("smearing") == "fermi-dirac", xc=ref.get("xc", "LDA_PW"))
     assert out["n_scf"] == ref["n_scf"]
     assert abs(out["E_per_atom"] - ref["E_per_atom"]) < 1e-10
     for a, b in zip(out["EigVal"], ref["EigVal"]):
