@@ -20,7 +20,7 @@ BUILD = HERE / "_build"
 LIB = HERE / "libcyclix_gpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["cx_stencil.cu", "cx_stencil_tma.cu", "cx_api.cu", "cx_linalg.cu", "cx_poisson.cu", "cx_scf.cu", "cx_noalloc.cu",
-           "cx_tcgen05.cu", "cx_nl_tc.cu"]
+           "cx_tcgen05.cu", "cx_nl_tc.cu", "cx_force.cu"]
 
 
 def nvcc() -> str:

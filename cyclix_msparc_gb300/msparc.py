@@ -66,6 +66,7 @@ class CyclixGPU:
         # the library's projector kernels hold 4 columns per atom: psp8 atoms with more are passed
         # as several atoms at the same position (the same operator, see split_projector_columns)
         nl_atoms, origin = split_projector_columns(S.Atom, 4)
+        self.nl_origin = np.asarray(origin, dtype=np.int64)
         atoms = (_lib.cx_atom * max(1, len(nl_atoms)))()
         for J, A in enumerate(nl_atoms):
             imgs = (_lib.cx_rc_image * max(1, A.n_image_rc))()
@@ -223,6 +224,32 @@ class CyclixGPU:
         e = np.zeros(self.N)
         check(self.lib, self.h, self.lib.cx_xc(self.h, _lib.XC[xc], dptr(rho), dptr(V), dptr(e)))
         return V, e
+
+    def nonlocal_force(self, occ, wkpt, occfac):
+        """Nonlocal part of the atomic forces (cx_nonlocal_force, src/atomicForce.m:254-300) from the
+        device-resident psi: ``occ`` packed like EigVal, ``wkpt`` one weight per block.  Returns
+        (n_atm, 3) for the atoms of ``S.Atom`` (the parts of an atom passed as several 4-column atoms
+        summed)."""
+        occ = np.ascontiguousarray(occ, dtype=np.float64).reshape(-1)
+        wkpt = np.ascontiguousarray(wkpt, dtype=np.float64).reshape(-1)
+        if occ.size != int(sum(self.Ns)) or wkpt.size != len(self.blocks):
+            raise ValueError(f"nonlocal_force: occ needs {int(sum(self.Ns))} values and wkpt {len(self.blocks)}")
+        nat = self.nl_origin.size
+        F = np.zeros(3 * max(nat, 1))
+        check(self.lib, self.h, self.lib.cx_nonlocal_force(self.h, dptr(occ), dptr(wkpt), float(occfac), dptr(F)))
+        parts = F[:3 * nat].reshape(3, nat).T
+        out = np.zeros((int(self.S.Atoms.shape[0]), 3))
+        np.add.at(out, self.nl_origin, parts)
+        return out
+
+    def gradient(self, f):
+        """Cartesian gradient (N, 3) of a real grid field at k = 0 (cx_gradient: S.grad_1..3 * f)."""
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
+        if f.size != self.N:
+            raise ValueError(f"gradient: f needs N = {self.N} values, got {f.size}")
+        D = np.zeros(3 * self.N)
+        check(self.lib, self.h, self.lib.cx_gradient(self.h, dptr(f), dptr(D)))
+        return D.reshape(3, self.N).T
 
     def scf(self, S, scf_tol=1e-6, poisson_tol=-1.0, max_scf=100, min_scf=3, rhoTrigger=4, maxit_poisson=1000,
             mixing_param=0.3, refine=None, fp64_tol=0.0):

@@ -18,6 +18,8 @@
  *                         nspin = 1, potential mixing) src/scf.m:1-327
  *   cx_xc               S = exchangeCorrelationPotential(S) (nspin = 1: LDA_PW, LDA_PZ, GGA_PBE)
  *                         src/exchangeCorrelationPotential.m:1-80
+ *   cx_nonlocal_force   the nonlocal term of S = atomicForce(S) src/atomicForce.m:254-300
+ *   cx_gradient         S.grad_1..3 * f (blochGradient(S,[0 0 0],d), src/initialization.m:743-745)
  *
  * The operator data that MATLAB keeps in the struct S (grid, FD weights,
  * quadrature weights, KB projector images) is handed over once in cx_create;
@@ -221,6 +223,24 @@ enum {
  * grad rho) with the same operators (src/exchangeCorrelationPotential.m:354-362); it needs theta
  * and z periodic.  Allocates and frees its device work arrays. */
 cx_status cx_xc(cx_handle h, int32_t xc, const double* rho, double* Vxc, double* e_xc);
+
+/* Nonlocal part of the atomic forces (src/atomicForce.m:254-300) from the device-resident psi of
+ * every block: for each block (Bloch vector k, weight wkpt[b], occupations occ packed like EigVal)
+ * the Bloch-summed projectors of every atom and their Cartesian gradients on the grid (the x / y
+ * pair with the wedge rotation across the theta wrap, Cychel/div_gradvec_cychel.m), and
+ *   F_J -= occfac 2 wkpt[b] sum_n occ_n sum_c gamma_c Re[conj(<psi_n|W chi_c>) (-<psi_n|W D chi_c>)].
+ * F is n_atm x 3, column-major, for the atoms of cx_create (an atom passed as several 4-column
+ * atoms gets one row per part; their sum is its force).  complex64 blocks are widened to
+ * complex128 for the products.  Allocates and frees its device work arrays (7 N x 4 n_atm complex
+ * values and one block of psi). */
+cx_status cx_nonlocal_force(cx_handle h, const double* occ, const double* wkpt, double occfac, double* F);
+
+/* Cartesian gradient of a real grid field at k = 0 (the S.grad_1, S.grad_2, S.grad_3 products
+ * src/atomicForce.m applies to phi and V_c): D_x = cos(phi) d_r - sin(phi)/r d_theta,
+ * D_y = sin(phi) d_r + cos(phi)/r d_theta, D_z = d_z - twist d_theta with phi = theta + twist z,
+ * order-2 FDn first-derivative stencils, zero beyond the radial walls, theta and z periodic.
+ * f: N values; Df: N x 3, column-major. */
+cx_status cx_gradient(cx_handle h, const double* f, double* Df);
 
 /* SCF parameters: the S fields read by src/scf.m (nspin = 1, potential mixing). */
 typedef struct {

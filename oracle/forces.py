@@ -114,6 +114,55 @@ def _rot_pow(R, p):
     return np.linalg.matrix_power(R, p) if p >= 0 else np.linalg.matrix_power(R.T, -p)
 
 
+def projector_fields(S, J, k):
+    """(Ck, R1, R2) of atom J at Bloch vector k, N x angnum each: the Bloch sum of the image
+    projectors, and the same weighted by ROT(1,1) and ROT(1,2) of each image's rotation
+    (src/atomicForce.m:265-277)."""
+    RotM1, RotM2 = rot_z(S.L2), rot_z(S.twist * S.L3)
+    A = S.Atom[J]
+    R1 = np.zeros((S.N, A.angnum), complex)
+    R2 = np.zeros((S.N, A.angnum), complex)
+    Ck = np.zeros((S.N, A.angnum), complex)
+    for img in A.rcImage:
+        disp = S.Atoms[J] - img.coordinates
+        ph = np.exp(-1j * float(np.dot(k, disp)))
+        ROT = _rot_pow(RotM1, int(round(disp[1] / S.L2))) @ _rot_pow(RotM2, int(round(disp[2] / S.L3)))
+        pos = img.rc_pos - 1
+        R1[pos] += ROT[0, 0] * img.Chi_mat * ph
+        R2[pos] += ROT[0, 1] * img.Chi_mat * ph
+        Ck[pos] += img.Chi_mat * ph
+    return Ck, R1, R2
+
+
+def projector_gradients(S, J, k, entries=None):
+    """(Ck, D_x, D_y, D_z) of atom J at Bloch vector k (src/atomicForce.m:278-280)."""
+    entries = entries or _grad_entries(S)
+    M1, M2 = vector_gradient_ops(S, k, entries)
+    Gz = bloch_gradients(S, k, entries)[2]
+    Ck, R1, R2 = projector_fields(S, J, k)
+    return Ck, M1 @ R1 + M2 @ R2, -(M1 @ R2) + M2 @ R1, Gz @ Ck
+
+
+def nonlocal_forces(S, kvecs, wkpt, psis, occ, occfac, entries=None):
+    """Nonlocal atomic forces (n_atm, 3) of src/atomicForce.m:254-300: per Bloch block b (vector
+    kvecs[b], weight wkpt[b], psi N x Ns, occupations occ[b]),
+    F_J -= occfac 2 w_b gamma^T Re[conj(<psi|W Ck>) * (-<psi|W D Ck>)] occ."""
+    entries = entries or _grad_entries(S)
+    F_nl = np.zeros((S.n_atm, 3))
+    for b, k in enumerate(kvecs):
+        psi = psis[b]
+        PsiW = (np.conj(psi) * S.W[:, None]).T                   # Ns x N
+        fk = np.zeros((S.n_atm, 3))
+        for J, A in enumerate(S.Atom):
+            Ck, DCx, DCy, DCz = projector_gradients(S, J, k, entries)
+            i1 = (np.conj(PsiW) @ np.conj(Ck)).T                  # angnum x Ns
+            for q, DC in enumerate((DCx, DCy, DCz)):
+                i2 = -(PsiW @ DC).T
+                fk[J, q] = float(A.gamma_Jl @ np.real(i1 * i2) @ occ[b])
+        F_nl -= occfac * 2 * wkpt[b] * fk
+    return F_nl
+
+
 def atomic_forces(d, psis, occ, phi):
     """Drift-free forces (n_atm, 3) in Ha/bohr of the converged SCF of a loaded deck ``d``: ``psis``
     and ``occ`` per Bloch block (W-normalised psi, N x Ns), ``phi`` the electrostatic potential.
@@ -156,34 +205,7 @@ def atomic_forces(d, psis, occ, phi):
             ROT = _rot_pow(RotM1, fac1) @ _rot_pow(RotM2, fac2)
             F_loc[J] += ROT @ fl
             F_cor[J] += ROT @ fc
-    # nonlocal part, per Bloch block
-    F_nl = np.zeros((S.n_atm, 3))
-    for b, k in enumerate(S.kptgrid):
-        M1, M2 = vector_gradient_ops(S, k, ent)
-        Gz = bloch_gradients(S, k, ent)[2]
-        psi = psis[b]
-        PsiW = (np.conj(psi) * S.W[:, None]).T                   # Ns x N
-        fk = np.zeros((S.n_atm, 3))
-        for J, A in enumerate(S.Atom):
-            R1 = np.zeros((S.N, A.angnum), complex)
-            R2 = np.zeros((S.N, A.angnum), complex)
-            Ck = np.zeros((S.N, A.angnum), complex)
-            for img in A.rcImage:
-                disp = S.Atoms[J] - img.coordinates
-                ph = np.exp(-1j * float(np.dot(k, disp)))
-                ROT = _rot_pow(RotM1, int(round(disp[1] / S.L2))) @ _rot_pow(RotM2, int(round(disp[2] / S.L3)))
-                pos = img.rc_pos - 1
-                R1[pos] += ROT[0, 0] * img.Chi_mat * ph
-                R2[pos] += ROT[0, 1] * img.Chi_mat * ph
-                Ck[pos] += img.Chi_mat * ph
-            DCx = M1 @ R1 + M2 @ R2
-            DCy = -(M1 @ R2) + M2 @ R1
-            DCz = Gz @ Ck
-            i1 = (np.conj(PsiW) @ np.conj(Ck)).T                  # angnum x Ns
-            for q, DC in enumerate((DCx, DCy, DCz)):
-                i2 = -(PsiW @ DC).T
-                fk[J, q] = float(A.gamma_Jl @ np.real(i1 * i2) @ occ[b])
-        F_nl -= S.occfac * 2 * S.wkpt[b] * fk
+    F_nl = nonlocal_forces(S, S.kptgrid, S.wkpt, psis, occ, S.occfac, ent)
     F = F_loc + F_cor + F_nl
     # drift-free forces: the mean force is removed along z, the translation a Cyclix cell has
     # (src/electronicGroundState.m:108-115)
