@@ -24,7 +24,8 @@ EXPORTS = ["cx_create", "cx_destroy", "cx_last_error", "cx_version", "cx_set_blo
            "cx_timer_start", "cx_timer_stop", "cx_profile_stencil", "cx_profile_read", "cx_launch_count",
            "cx_host_register", "cx_host_unregister", "cx_hpsi_noalloc", "cx_profile_read_apply", "cx_profile_read_contract", "cx_set_nl_kernels", "cx_eig_fallback_count", "cx_scf", "cx_refine_eigenvalues", "cx_set_device",
            "cx_eigsolver_full", "cx_eigsolver_full_host", "cx_scf_init", "cx_scf_step", "cx_scf_finish",
-           "cx_eig_hermitian_count", "cx_stencil_config", "cx_xc", "cx_nonlocal_force", "cx_gradient"]
+           "cx_eig_hermitian_count", "cx_stencil_config", "cx_xc", "cx_nonlocal_force", "cx_gradient",
+           "cx_field_projections"]
 
 
 class cx_grid(C.Structure):
@@ -132,6 +133,7 @@ def load(build_if_missing: bool = True):
         "cx_xc": ([h, C.c_int32, dp, dp, dp], C.c_int32),
         "cx_nonlocal_force": ([h, dp, dp, C.c_double, dp], C.c_int32),
         "cx_gradient": ([h, dp, dp], C.c_int32),
+        "cx_field_projections": ([h, dp, C.c_int32, dp, dp], C.c_int32),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

@@ -160,3 +160,38 @@ extern "C" cx_status cx_gradient(cx_handle h, const double* f, double* Df) {
   CX_TRY_CUDA(h, cudaStreamSynchronize(st));
   return CX_OK;
 }
+
+extern "C" cx_status cx_field_projections(cx_handle h, const double* f, int32_t nvec, const double* A, double* out) {
+  if (!h) return CX_ERR_ARG;
+  if (!f || (nvec > 0 && (!A || !out)) || nvec < 0) { h->err = "cx_field_projections: f, A and out are required, nvec >= 0"; return CX_ERR_ARG; }
+  if (h->grid.BCy != 0 || h->grid.BCz != 0) { h->err = "cx_field_projections: theta and z must be periodic (BCy = BCz = 0)"; return CX_ERR_ARG; }
+  if (nvec == 0) return CX_OK;
+  const int N = h->g.N;
+  const cudaStream_t st = h->stream;
+  ForceScratch sc;
+  const size_t n_f = (size_t)N, n_D = 3 * (size_t)N, n_A = (size_t)nvec * N, n_o = 3 * (size_t)nvec;
+  if (cudaMalloc(&sc.base, (n_f + n_D + n_A + n_o) * 8) != cudaSuccess) {
+    cudaGetLastError();
+    h->err = "cx_field_projections: device allocation failed";
+    return CX_ERR_NOMEM;
+  }
+  double* d_f = (double*)sc.base;
+  double* d_D = d_f + n_f;
+  double* d_A = d_D + n_D;
+  double* d_o = d_A + n_A;
+  const force::ForceGrid g = force_grid(h);
+  CX_TRY_CUDA(h, cudaMemcpyAsync(d_f, f, n_f * 8, cudaMemcpyHostToDevice, st));
+  CX_TRY_CUDA(h, cudaMemcpyAsync(d_A, A, n_A * 8, cudaMemcpyHostToDevice, st));
+  k_real_grad<<<grid_for(N), 256, 0, st>>>(N, g, d_f, d_D);
+  h->launches++;
+  CX_TRY_CUDA(h, cudaGetLastError());
+  const double one = 1.0, zero = 0.0;
+  if (cublasSetMathMode(h->cublas, CUBLAS_DEFAULT_MATH) != CUBLAS_STATUS_SUCCESS ||
+      cublasDgemm(h->cublas, CUBLAS_OP_T, CUBLAS_OP_N, nvec, 3, N, &one, d_A, N, d_D, N, &zero, d_o, nvec) != CUBLAS_STATUS_SUCCESS) {
+    h->err = "cx_field_projections: cublasDgemm failed";
+    return CX_ERR_LIB;
+  }
+  CX_TRY_CUDA(h, cudaMemcpyAsync(out, d_o, n_o * 8, cudaMemcpyDeviceToHost, st));
+  CX_TRY_CUDA(h, cudaStreamSynchronize(st));
+  return CX_OK;
+}

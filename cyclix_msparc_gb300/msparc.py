@@ -251,6 +251,17 @@ class CyclixGPU:
         check(self.lib, self.h, self.lib.cx_gradient(self.h, dptr(f), dptr(D)))
         return D.reshape(3, self.N).T
 
+    def field_projections(self, f, A):
+        """(nvec, 3): the projections A[v] . D_d f of the Cartesian gradient of a real grid field on
+        the rows of ``A`` (nvec x N) (cx_field_projections)."""
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        if f.size != self.N or A.ndim != 2 or A.shape[1] != self.N:
+            raise ValueError(f"field_projections: f needs N = {self.N} values and A shape (nvec, {self.N})")
+        out = np.zeros(3 * max(A.shape[0], 1))
+        check(self.lib, self.h, self.lib.cx_field_projections(self.h, dptr(f), int(A.shape[0]), dptr(A), dptr(out)))
+        return out[:3 * A.shape[0]].reshape(3, A.shape[0]).T
+
     def scf(self, S, scf_tol=1e-6, poisson_tol=-1.0, max_scf=100, min_scf=3, rhoTrigger=4, maxit_poisson=1000,
             mixing_param=0.3, refine=None, fp64_tol=0.0):
         """Full SCF on the device-resident psi (cx_scf); returns (result, EigVal packed, rho, Veff, history).

@@ -20,6 +20,7 @@
  *                         src/exchangeCorrelationPotential.m:1-80
  *   cx_nonlocal_force   the nonlocal term of S = atomicForce(S) src/atomicForce.m:254-300
  *   cx_gradient         S.grad_1..3 * f (blochGradient(S,[0 0 0],d), src/initialization.m:743-745)
+ *   cx_field_projections  the grid sums of the local and correction forces src/atomicForce.m:111-127
  *
  * The operator data that MATLAB keeps in the struct S (grid, FD weights,
  * quadrature weights, KB projector images) is handed over once in cx_create;
@@ -241,6 +242,12 @@ cx_status cx_nonlocal_force(cx_handle h, const double* occ, const double* wkpt, 
  * order-2 FDn first-derivative stencils, zero beyond the radial walls, theta and z periodic.
  * f: N values; Df: N x 3, column-major. */
 cx_status cx_gradient(cx_handle h, const double* f, double* Df);
+
+/* Projections of the gradient of a real grid field on nvec grid vectors: out (nvec x 3,
+ * column-major) = A^T [D_x f, D_y f, D_z f], A N x nvec column-major, D as cx_gradient.  The local
+ * and correction terms of src/atomicForce.m:111-127 are such projections of D phi and D V_c on
+ * per-atom sums of W bJ over the atom's image boxes (the host set-up reduces them so). */
+cx_status cx_field_projections(cx_handle h, const double* f, int32_t nvec, const double* A, double* out);
 
 /* SCF parameters: the S fields read by src/scf.m (nspin = 1, potential mixing). */
 typedef struct {

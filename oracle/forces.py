@@ -134,11 +134,13 @@ def projector_fields(S, J, k):
     return Ck, R1, R2
 
 
-def projector_gradients(S, J, k, entries=None):
-    """(Ck, D_x, D_y, D_z) of atom J at Bloch vector k (src/atomicForce.m:278-280)."""
-    entries = entries or _grad_entries(S)
-    M1, M2 = vector_gradient_ops(S, k, entries)
-    Gz = bloch_gradients(S, k, entries)[2]
+def projector_gradients(S, J, k, entries=None, ops=None):
+    """(Ck, D_x, D_y, D_z) of atom J at Bloch vector k (src/atomicForce.m:278-280); ``ops`` the
+    (M1, M2, G_z) of k when already built."""
+    if ops is None:
+        entries = entries or _grad_entries(S)
+        ops = vector_gradient_ops(S, k, entries) + (bloch_gradients(S, k, entries)[2],)
+    M1, M2, Gz = ops
     Ck, R1, R2 = projector_fields(S, J, k)
     return Ck, M1 @ R1 + M2 @ R2, -(M1 @ R2) + M2 @ R1, Gz @ Ck
 
@@ -153,8 +155,9 @@ def nonlocal_forces(S, kvecs, wkpt, psis, occ, occfac, entries=None):
         psi = psis[b]
         PsiW = (np.conj(psi) * S.W[:, None]).T                   # Ns x N
         fk = np.zeros((S.n_atm, 3))
+        ops = vector_gradient_ops(S, k, entries) + (bloch_gradients(S, k, entries)[2],)
         for J, A in enumerate(S.Atom):
-            Ck, DCx, DCy, DCz = projector_gradients(S, J, k, entries)
+            Ck, DCx, DCy, DCz = projector_gradients(S, J, k, ops=ops)
             i1 = (np.conj(PsiW) @ np.conj(Ck)).T                  # angnum x Ns
             for q, DC in enumerate((DCx, DCy, DCz)):
                 i2 = -(PsiW @ DC).T

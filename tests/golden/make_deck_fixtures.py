@@ -46,6 +46,12 @@ def save(name, rel, root):
         img_pos=np.concatenate([img.rc_pos for A in S.Atom for img in A.rcImage]).astype(np.int32),
         img_chi=np.concatenate([img.Chi_mat.reshape(-1, order="F") for A in S.Atom for img in A.rcImage]),
         xc=np.array(S.extra.get("xc", "LDA_PW")),
+        # the local-potential part of the set-up, for the force tests: per atom type the valence
+        # charge, the psp8 radial grid with its local potential and isolated-atom density, and the
+        # pseudocharge box half-widths; per atom its type
+        atom_type=np.asarray(S.extra["atom_type"], dtype=np.int64),
+        psp_Z=np.array([P.Z for P in d.psps]), rb=np.array([list(r) for r in d.rb]),
+        **{f"psp{t}_{k}": getattr(P, k) for t, P in enumerate(d.psps) for k in ("r", "Vloc", "rho_iso")},
     )
     path = os.path.join(HERE, f"deck_{name}.npz")
     np.savez_compressed(path, **arrays)
@@ -83,6 +89,23 @@ def load(name):
     S.elec_T_type, S.occfac, S.n_atm = int(elec_T_type), float(occfac), int(n_atm)
     S.extra.update(deck=name, xc=str(z["xc"]) if "xc" in z.files else "LDA_PW")
     return S, float(scf_tol), float(poisson_tol), float(e_ref)
+
+
+def load_force_deck(name):
+    """A deck object for the force code (``forces.local_force_setup``, oracle/forces.py) rebuilt from a
+    saved set-up that holds the local-potential tables: S, psps (valence charge, radial grid, local
+    potential, isolated-atom density per type), rb, and the pseudocharge set-up (b, b_ref, V_c, ...)
+    recomputed from them.  Returns (deck, scf_tol, poisson_tol, printed free energy per atom)."""
+    from types import SimpleNamespace
+    from cyclix_msparc_gb300.deck import pseudocharges
+    S, scf_tol, poisson_tol, e_ref = load(name)
+    z = np.load(os.path.join(HERE, f"deck_{name}.npz"))
+    psps = [SimpleNamespace(Z=float(Z), r=z[f"psp{t}_r"], Vloc=z[f"psp{t}_Vloc"], rho_iso=z[f"psp{t}_rho_iso"])
+            for t, Z in enumerate(z["psp_Z"])]
+    rb = [tuple(float(v) for v in r) for r in z["rb"]]
+    S.extra["atom_type"] = z["atom_type"].astype(int)
+    pc = pseudocharges(S, psps, S.extra["atom_type"], rb)
+    return SimpleNamespace(S=S, psps=psps, rb=rb, pseudo=pc), scf_tol, poisson_tol, e_ref
 
 
 def oracle_reference(name, scf_tol=1e-8, poisson_tol=1e-10, max_scf=60):
