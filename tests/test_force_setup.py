@@ -39,3 +39,13 @@ def test_occupations_match_oracle():
     ev = np.linspace(-0.5, 0.5, 101)
     for T in (0, 1):
         assert np.max(np.abs(occupations(ev, 0.03, 50.0, T) - _occ(ev, 0.03, 50.0, T))) < 1e-15
+
+
+def test_force_deck_rebuilds_the_saved_setup():
+    """The local-potential tables of the fixture reproduce its saved pseudocharge set-up exactly."""
+    from golden.make_deck_fixtures import load
+    d, _, _, _ = load_force_deck("CNT_chiral")
+    S0 = load("CNT_chiral")[0]
+    assert np.array_equal(d.pseudo["b"], S0.b)
+    assert np.array_equal(d.pseudo["rho_at"], S0.rho_at)
+    assert d.pseudo["Eself"] == S0.Eself and d.pseudo["E_corr"] == S0.E_corr
